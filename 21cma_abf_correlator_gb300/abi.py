@@ -1,0 +1,194 @@
+"""ctypes view of libcorr_cuda.so: structures, status codes, entry points.
+
+The structures mirror include/corr_cuda.h field for field (the same layouts the
+reference's Rust mirror pins, corr-rs/src/ffi.rs:63-160); sizes are asserted at
+import so a header change cannot go unnoticed.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "lib" / "libcorr_cuda.so"
+
+CORR_ABI_VERSION = 7
+CORR_MAX_DEVICES = 8
+CORR_SPLIT_BASELINE_RANGE = 0
+CORR_SPLIT_PAIR_COVERING = 1
+CORR_SPLIT_TIME_SLICE = 2
+
+CORR_X_PLAIN_FP32 = 0
+CORR_X_TC_FP16 = 1
+CORR_X_TC_FP16_SPLIT = 2
+
+STATUS_NAMES = {
+    0: "CORR_OK",
+    1: "CORR_ERR_ARG",
+    2: "CORR_ERR_ABI",
+    3: "CORR_ERR_CUDA",
+    4: "CORR_ERR_CUFFT",
+    5: "CORR_ERR_STATE",
+    6: "CORR_ERR_BUSY",
+    7: "CORR_ERR_NOMEM",
+    8: "CORR_ERR_NOT_IMPL",
+    9: "CORR_ERR_INTERNAL",
+}
+globals().update({name: code for code, name in STATUS_NAMES.items()})
+
+
+class corr_config(C.Structure):
+    _fields_ = [
+        ("abi_version", C.c_uint32),
+        ("struct_size", C.c_uint32),
+        ("device_id", C.c_int32),
+        ("n_station", C.c_int32),
+        ("n_freq", C.c_int32),
+        ("frames_per_slot", C.c_int32),
+        ("chunk_frames", C.c_int32),
+        ("block_slots", C.c_int32),
+        ("rows_per_fetch", C.c_int32),
+        ("n_devices", C.c_int32),
+        ("devices", C.c_int32 * CORR_MAX_DEVICES),
+        ("split_mode", C.c_int32),
+    ]
+
+
+class corr_device_plan(C.Structure):
+    _fields_ = [
+        ("device_id", C.c_int32),
+        ("n_station_resident", C.c_int32),
+        ("first_baseline", C.c_int32),
+        ("n_baseline", C.c_int32),
+        ("contiguous", C.c_int32),
+    ]
+
+
+class corr_device_stats(C.Structure):
+    _fields_ = [
+        ("device_id", C.c_int32),
+        ("bytes_h2d", C.c_uint64),
+        ("bytes_d2h", C.c_uint64),
+        ("transfers", C.c_uint64),
+        ("ns_accumulate", C.c_uint64),
+        ("ns_slot_free", C.c_uint64),
+        ("ns_row_end", C.c_uint64),
+        ("ns_rows_wait", C.c_uint64),
+        ("ns_fetch", C.c_uint64),
+    ]
+
+
+class corr_staging(C.Structure):
+    _fields_ = [
+        ("base", C.POINTER(C.c_int8)),
+        ("frame_stride", C.c_size_t),
+        ("slot_stride", C.c_size_t),
+        ("total_bytes", C.c_size_t),
+        ("validity_offset", C.c_size_t),
+        ("validity_bytes_per_slot", C.c_size_t),
+    ]
+
+
+class corrx_params(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_uint32),
+        ("n_station", C.c_int32),
+        ("n_freq", C.c_int32),
+        ("max_frames", C.c_int32),
+        ("xmode", C.c_int32),
+        ("device_id", C.c_int32),
+    ]
+
+
+# Layouts pinned by the reference's Rust mirror (ffi.rs compile-time asserts).
+assert C.sizeof(corr_config) == 76
+assert C.sizeof(corr_device_plan) == 20
+assert C.sizeof(corr_device_stats) == 72
+assert C.sizeof(corr_staging) == 48
+
+NOTIFY_FN = C.CFUNCTYPE(None, C.c_void_p)
+
+# name -> (restype, argtypes); every symbol include/*.h declares.
+SIGNATURES = {
+    "corr_abi_banner": (C.c_char_p, []),
+    "corr_last_error": (C.c_char_p, []),
+    "corr_create": (C.c_int, [C.POINTER(corr_config), C.POINTER(C.c_void_p)]),
+    "corr_destroy": (C.c_int, [C.c_void_p]),
+    "corr_staging_info": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(corr_staging)]),
+    "corr_row_accumulate": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32]),
+    "corr_row_slot_free": (C.c_int, [C.c_void_p, C.c_int64]),
+    "corr_row_slot_free_submit": (C.c_int, [C.c_void_p, C.c_int64, NOTIFY_FN, C.c_void_p]),
+    "corr_row_slot_free_finish": (C.c_int, [C.c_void_p, C.c_int64]),
+    "corr_row_end": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "corr_rows_wait": (C.c_int, [C.c_void_p]),
+    "corr_rows_wait_submit": (C.c_int, [C.c_void_p, NOTIFY_FN, C.c_void_p]),
+    "corr_rows_ready": (C.c_int, [C.c_void_p]),
+    "corr_rows_pending": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "corr_rows_fetch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_int32)]),
+    "corr_rows_fetch_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t,
+                                         C.POINTER(C.c_int32), NOTIFY_FN, C.c_void_p]),
+    "corr_rows_fetch_ready": (C.c_int, [C.c_void_p]),
+    "corr_n_baseline": (C.c_int32, [C.c_int32]),
+    "corr_baseline_pairs": (C.c_int, [C.c_int32, C.POINTER(C.c_int32), C.c_int32]),
+    "corr_n_devices": (C.c_int32, [C.c_void_p]),
+    "corr_device_plan_get": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(corr_device_plan)]),
+    "corr_device_stations": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.c_int32]),
+    "corr_device_baselines": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.c_int32]),
+    "corr_device_stats_get": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(corr_device_stats)]),
+    "corr_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
+    "corr_host_free": (None, [C.c_void_p]),
+    # corr_gb300.h
+    "corr_set_xengine": (C.c_int, [C.c_void_p, C.c_int32]),
+    "corrx_create": (C.c_int, [C.POINTER(corrx_params), C.POINTER(C.c_void_p)]),
+    "corrx_destroy": (C.c_int, [C.c_void_p]),
+    "corrx_accumulate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p,
+                                   C.c_size_t, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "corrx_scale": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "corrx_check": (C.c_int, [C.c_void_p]),
+    "corrx_run_fengine": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p,
+                                    C.c_size_t, C.c_int32, C.c_int32, C.c_void_p]),
+    "corrx_run_xengine": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    "corrx_selftest_watchdog": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
+}
+
+_lib: C.CDLL | None = None
+
+
+def load(path: Path | str | None = None) -> C.CDLL:
+    """Load the in-tree libcorr_cuda.so (built by build.py) and bind every entry point.
+
+    Raises if the library is missing: there is no fallback implementation.
+    """
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path is not None else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(
+            f"{p} is missing: build the CUDA library first (python -c 'import __graft_entry__ as g; "
+            "g.build()'); this package has no CPU fallback")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class CorrError(RuntimeError):
+    """A failing corr_status together with corr_last_error()."""
+
+    def __init__(self, status: int, what: str, message: str):
+        self.status = status
+        self.status_name = STATUS_NAMES.get(status, f"status {status}")
+        self.message = message
+        super().__init__(f"{what} failed: {self.status_name} ({message})")
+
+
+def check(status: int, what: str) -> None:
+    if status != 0:
+        msg = load().corr_last_error().decode(errors="replace")
+        raise CorrError(status, what, msg)

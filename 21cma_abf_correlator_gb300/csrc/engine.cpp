@@ -1,0 +1,301 @@
+// engine.cpp -- FX plan: device buffers + the F/X launch sequence, and the
+// device-resident extension entry points declared in corr_gb300.h.
+//
+// One pass of the plan over `ft` frames is two launches on the caller's stream:
+//   F-engine: ft*n_station int8 frames -> spectra y   (fengine.cu)
+//   X-engine: spectra y -> acc += visibilities        (xengine.cu / xengine_tc.cu)
+// The spectra buffer is sized for max_frames frames; longer requests are split
+// into passes. This is the work the reference does per chunk in gpu_accumulate
+// (corr-cuda/src/kernels.cu:806-845), minus the host copies, which belong to the
+// caller (abi.cpp for the staging ring).
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "engine.h"
+
+namespace corrgb {
+
+std::string &last_error() {
+    static thread_local std::string s;
+    return s;
+}
+
+corr_status fail(corr_status st, const std::string &msg) {
+    last_error() = msg;
+    return st;
+}
+
+corr_status failf(corr_status st, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    last_error() = buf;
+    return st;
+}
+
+corr_status cuda_check(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return CORR_OK;
+    return fail(CORR_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorName(e) + ": " + cudaGetErrorString(e));
+}
+
+static bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+
+corr_status check_geometry(int n_station, int n_freq) {
+    if (n_station < 1) return fail(CORR_ERR_ARG, "n_station must be >= 1");
+    if (n_station * (n_station + 1) / 2 > 1024)
+        return failf(CORR_ERR_ARG,
+                     "n_station=%d gives %d baselines; at most 1024 (n_station <= 44) "
+                     "are supported",
+                     n_station, n_station * (n_station + 1) / 2);
+    if (n_freq < 1) return fail(CORR_ERR_ARG, "n_freq must be >= 1");
+    if (!is_pow2(n_freq) || n_freq < 512 || n_freq > 16384) {
+        if (n_freq % 2048 == 0)
+            return failf(CORR_ERR_NOT_IMPL,
+                         "n_freq=%d: the F-engine transforms power-of-two frames only "
+                         "(n_freq in 512..16384)",
+                         n_freq);
+        return failf(CORR_ERR_ARG, "n_freq=%d is not a power of two in [512, 16384]", n_freq);
+    }
+    return CORR_OK;
+}
+
+corr_status fxplan_create(int device, int n_station, int n_freq, int max_frames, int xmode,
+                          FxPlan **out) {
+    if (out == nullptr) return fail(CORR_ERR_ARG, "fxplan_create: out is NULL");
+    *out = nullptr;
+    corr_status st = check_geometry(n_station, n_freq);
+    if (st != CORR_OK) return st;
+    if (max_frames < 1) return fail(CORR_ERR_ARG, "max_frames must be >= 1");
+    if (xmode != CORR_X_PLAIN_FP32 && xmode != CORR_X_TC_FP16 && xmode != CORR_X_TC_FP16_SPLIT)
+        return failf(CORR_ERR_ARG, "unknown X-engine mode %d", xmode);
+    if ((st = cuda_check(cudaSetDevice(device), "cudaSetDevice")) != CORR_OK) return st;
+
+    FxPlan *p = new (std::nothrow) FxPlan();
+    if (p == nullptr) return fail(CORR_ERR_NOMEM, "fxplan_create: out of host memory");
+    p->device = device;
+    p->n_station = n_station;
+    p->n_freq = n_freq;
+    p->n_baseline = n_station * (n_station + 1) / 2;
+    p->max_frames = max_frames;
+    p->xmode = xmode;
+    if ((st = cuda_check(cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount,
+                                                device),
+                         "cudaDeviceGetAttribute(SM count)")) != CORR_OK) {
+        delete p;
+        return st;
+    }
+    const size_t y_bytes = static_cast<size_t>(max_frames) * n_station * n_freq * sizeof(float2);
+    if (cudaMalloc(&p->d_y, y_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        delete p;
+        return failf(CORR_ERR_NOMEM, "cudaMalloc(spectra, %zu bytes) failed", y_bytes);
+    }
+    if ((st = cuda_check(cudaMalloc(&p->d_err, sizeof(int)), "cudaMalloc(watchdog)")) !=
+            CORR_OK ||
+        (st = cuda_check(cudaMemset(p->d_err, 0, sizeof(int)), "cudaMemset(watchdog)")) !=
+            CORR_OK ||
+        (st = fengine_prepare(n_freq, &p->tw)) != CORR_OK) {
+        fxplan_destroy(p);
+        return st;
+    }
+    *out = p;
+    return CORR_OK;
+}
+
+void fxplan_destroy(FxPlan *p) {
+    if (p == nullptr) return;
+    cudaSetDevice(p->device);
+    fengine_release(&p->tw);
+    if (p->d_y) cudaFree(p->d_y);
+    if (p->d_err) cudaFree(p->d_err);
+    delete p;
+}
+
+corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_stride,
+                              size_t frame_stride, const uint8_t *mask,
+                              size_t mask_station_stride, int mask_bit0, int frames,
+                              float2 *acc, cudaStream_t stream) {
+    if (frames < 0) return fail(CORR_ERR_ARG, "frames must be >= 0");
+    const size_t frame_bytes = 2u * static_cast<size_t>(p->n_freq);
+    if (frame_stride < frame_bytes)
+        return fail(CORR_ERR_ARG, "frame_stride is shorter than a frame");
+    if ((reinterpret_cast<uintptr_t>(samples) | station_stride | frame_stride) % 16 != 0)
+        return fail(CORR_ERR_ARG,
+                    "samples, station_stride and frame_stride must be 16-byte aligned "
+                    "(the F-engine loads frames with TMA bulk copies)");
+    for (int f0 = 0; f0 < frames; f0 += p->max_frames) {
+        const int ft = frames - f0 < p->max_frames ? frames - f0 : p->max_frames;
+        FengineArgs fa{};
+        fa.samples = samples + static_cast<size_t>(f0) * frame_stride;
+        fa.station_stride = station_stride;
+        fa.frame_stride = frame_stride;
+        fa.mask = mask;
+        fa.mask_station_stride = mask_station_stride;
+        fa.mask_bit0 = mask_bit0 + f0;
+        fa.n_station = p->n_station;
+        fa.frames = ft;
+        fa.y = p->d_y;
+        fa.err = p->d_err;
+        corr_status st = fengine_launch(p->n_freq, p->tw, fa, p->num_sms, stream);
+        if (st != CORR_OK) return st;
+        XengineArgs xa{};
+        xa.y = p->d_y;
+        xa.n_station = p->n_station;
+        xa.n_freq = p->n_freq;
+        xa.frames = ft;
+        xa.acc = acc;
+        xa.err = p->d_err;
+        if (p->xmode == CORR_X_PLAIN_FP32)
+            st = xengine_plain_launch(xa, p->num_sms, stream);
+        else
+            st = xengine_tc_launch(xa, p->xmode == CORR_X_TC_FP16_SPLIT, p->num_sms, stream);
+        if (st != CORR_OK) return st;
+    }
+    return CORR_OK;
+}
+
+corr_status fxplan_check(FxPlan *p) {
+    corr_status st = cuda_check(cudaSetDevice(p->device), "cudaSetDevice");
+    if (st != CORR_OK) return st;
+    if ((st = cuda_check(cudaDeviceSynchronize(), "cudaDeviceSynchronize")) != CORR_OK) return st;
+    int code = 0;
+    if ((st = cuda_check(cudaMemcpy(&code, p->d_err, sizeof(int), cudaMemcpyDeviceToHost),
+                         "cudaMemcpy(watchdog)")) != CORR_OK)
+        return st;
+    if (code != kErrNone) {
+        cudaMemset(p->d_err, 0, sizeof(int));
+        return failf(CORR_ERR_INTERNAL,
+                     "device watchdog tripped (code %d): a bounded wait inside a kernel ran "
+                     "out and the kernel returned early; results of that launch are invalid",
+                     code);
+    }
+    return CORR_OK;
+}
+
+} // namespace corrgb
+
+using namespace corrgb;
+
+extern "C" corr_status corrx_create(const corrx_params *prm, void **out_eng) {
+    if (out_eng == nullptr) return fail(CORR_ERR_ARG, "out_eng is NULL");
+    *out_eng = nullptr;
+    if (prm == nullptr) return fail(CORR_ERR_ARG, "params is NULL");
+    if (prm->struct_size != sizeof(corrx_params))
+        return failf(CORR_ERR_ABI, "corrx_params.struct_size=%u, expected %zu", prm->struct_size,
+                     sizeof(corrx_params));
+    int ndev = 0;
+    corr_status st = cuda_check(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
+    if (st != CORR_OK) return st;
+    if (prm->device_id < 0 || prm->device_id >= ndev)
+        return failf(CORR_ERR_ARG, "device_id=%d but %d device(s) are visible", prm->device_id,
+                     ndev);
+    FxPlan *p = nullptr;
+    st = fxplan_create(prm->device_id, prm->n_station, prm->n_freq, prm->max_frames, prm->xmode,
+                       &p);
+    if (st != CORR_OK) return st;
+    *out_eng = p;
+    return CORR_OK;
+}
+
+extern "C" corr_status corrx_destroy(void *eng) {
+    fxplan_destroy(static_cast<FxPlan *>(eng));
+    return CORR_OK;
+}
+
+extern "C" corr_status corrx_accumulate(void *eng, const int8_t *d_samples,
+                                        size_t station_stride, size_t frame_stride,
+                                        const uint8_t *d_mask, size_t mask_station_stride,
+                                        int32_t mask_bit0, int32_t frames, void *d_acc,
+                                        void *stream) {
+    FxPlan *p = static_cast<FxPlan *>(eng);
+    if (p == nullptr) return fail(CORR_ERR_ARG, "eng is NULL");
+    if (d_samples == nullptr || d_acc == nullptr)
+        return fail(CORR_ERR_ARG, "d_samples and d_acc must not be NULL");
+    if (mask_bit0 < 0) return fail(CORR_ERR_ARG, "mask_bit0 must be >= 0");
+    corr_status st = cuda_check(cudaSetDevice(p->device), "cudaSetDevice");
+    if (st != CORR_OK) return st;
+    return fxplan_accumulate(p, d_samples, station_stride, frame_stride, d_mask,
+                             mask_station_stride, mask_bit0, frames,
+                             static_cast<float2 *>(d_acc), static_cast<cudaStream_t>(stream));
+}
+
+extern "C" corr_status corrx_scale(void *eng, void *d_acc, uint64_t frames, void *stream) {
+    FxPlan *p = static_cast<FxPlan *>(eng);
+    if (p == nullptr) return fail(CORR_ERR_ARG, "eng is NULL");
+    if (frames == 0) return fail(CORR_ERR_ARG, "frames must be > 0");
+    corr_status st = cuda_check(cudaSetDevice(p->device), "cudaSetDevice");
+    if (st != CORR_OK) return st;
+    return scale_launch(static_cast<float2 *>(d_acc),
+                        static_cast<size_t>(p->n_baseline) * p->n_freq,
+                        1.0f / static_cast<float>(frames), static_cast<cudaStream_t>(stream));
+}
+
+extern "C" corr_status corrx_run_fengine(void *eng, const int8_t *d_samples,
+                                         size_t station_stride, size_t frame_stride,
+                                         const uint8_t *d_mask, size_t mask_station_stride,
+                                         int32_t mask_bit0, int32_t frames, void *stream) {
+    FxPlan *p = static_cast<FxPlan *>(eng);
+    if (p == nullptr) return fail(CORR_ERR_ARG, "eng is NULL");
+    if (d_samples == nullptr) return fail(CORR_ERR_ARG, "d_samples is NULL");
+    if (frames < 0 || frames > p->max_frames)
+        return failf(CORR_ERR_ARG, "frames=%d outside [0, max_frames=%d]", frames, p->max_frames);
+    if ((reinterpret_cast<uintptr_t>(d_samples) | station_stride | frame_stride) % 16 != 0)
+        return fail(CORR_ERR_ARG, "samples and strides must be 16-byte aligned");
+    corr_status st = cuda_check(cudaSetDevice(p->device), "cudaSetDevice");
+    if (st != CORR_OK) return st;
+    FengineArgs fa{};
+    fa.samples = d_samples;
+    fa.station_stride = station_stride;
+    fa.frame_stride = frame_stride;
+    fa.mask = d_mask;
+    fa.mask_station_stride = mask_station_stride;
+    fa.mask_bit0 = mask_bit0;
+    fa.n_station = p->n_station;
+    fa.frames = frames;
+    fa.y = p->d_y;
+    fa.err = p->d_err;
+    return fengine_launch(p->n_freq, p->tw, fa, p->num_sms, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" corr_status corrx_run_xengine(void *eng, int32_t frames, void *d_acc, void *stream) {
+    FxPlan *p = static_cast<FxPlan *>(eng);
+    if (p == nullptr) return fail(CORR_ERR_ARG, "eng is NULL");
+    if (d_acc == nullptr) return fail(CORR_ERR_ARG, "d_acc is NULL");
+    if (frames < 0 || frames > p->max_frames)
+        return failf(CORR_ERR_ARG, "frames=%d outside [0, max_frames=%d]", frames, p->max_frames);
+    corr_status st = cuda_check(cudaSetDevice(p->device), "cudaSetDevice");
+    if (st != CORR_OK) return st;
+    XengineArgs xa{};
+    xa.y = p->d_y;
+    xa.n_station = p->n_station;
+    xa.n_freq = p->n_freq;
+    xa.frames = frames;
+    xa.acc = static_cast<float2 *>(d_acc);
+    xa.err = p->d_err;
+    if (p->xmode == CORR_X_PLAIN_FP32)
+        return xengine_plain_launch(xa, p->num_sms, static_cast<cudaStream_t>(stream));
+    return xengine_tc_launch(xa, p->xmode == CORR_X_TC_FP16_SPLIT, p->num_sms,
+                             static_cast<cudaStream_t>(stream));
+}
+
+extern "C" corr_status corrx_selftest_watchdog(void *eng, int64_t budget_cycles, void *stream) {
+    FxPlan *p = static_cast<FxPlan *>(eng);
+    if (p == nullptr) return fail(CORR_ERR_ARG, "eng is NULL");
+    if (budget_cycles < 1 || budget_cycles > 4000000000LL)
+        return fail(CORR_ERR_ARG, "budget_cycles must be in [1, 4e9]");
+    corr_status st = cuda_check(cudaSetDevice(p->device), "cudaSetDevice");
+    if (st != CORR_OK) return st;
+    return watchdog_selftest_launch(p->d_err, budget_cycles, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" corr_status corrx_check(void *eng) {
+    FxPlan *p = static_cast<FxPlan *>(eng);
+    if (p == nullptr) return fail(CORR_ERR_ARG, "eng is NULL");
+    return fxplan_check(p);
+}

@@ -1,0 +1,128 @@
+// engine.h -- internal interface between the C ABI layer (abi.cpp), the
+// device-resident extension API and the CUDA translation units.
+//
+// The reference splits its library the same way (corr-cuda/src/gpu_internal.h
+// between corr_cuda.cpp and kernels.cu); the contents here are this engine's own:
+// an FX plan (F-engine FFT + X-engine) that works on device pointers, and the
+// staged pipeline (streams, events, row stack) the ABI drives.
+
+#ifndef CORR_GB300_ENGINE_H
+#define CORR_GB300_ENGINE_H
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "corr_cuda.h"
+#include "corr_gb300.h"
+
+namespace corrgb {
+
+/// Thread-local failure message returned by corr_last_error().
+std::string &last_error();
+corr_status fail(corr_status st, const std::string &msg);
+corr_status failf(corr_status st, const char *fmt, ...);
+corr_status cuda_check(cudaError_t e, const char *what);
+
+/// Watchdog codes a kernel writes into FxPlan::d_err when a bounded wait ran out.
+enum : int {
+    kErrNone = 0,
+    kErrFengineCopyTimeout = 1,
+    kErrXengineTmemTimeout = 2,
+    kErrXengineMmaTimeout = 3,
+    kErrSelftestTimeout = 4,
+};
+
+/// Twiddle tables, all computed on the host in double precision (libm) and
+/// rounded once to float.
+///   pass_lo[u]  = exp(-2*pi*i*u/M)        u in [0, 64)
+///   pass_hi[u]  = exp(-2*pi*i*64*u/M)     u in [0, M/64)
+///   post_lo[k]  = exp(-pi*i*k/M)          k in [0, 64)
+///   post_hi[k]  = exp(-pi*i*64*k/M)       k in [0, M/128 + 1)
+/// so exp(-2*pi*i*u/M) = pass_lo[u%64]*pass_hi[u/64] (u < M) and the real-FFT
+/// split twiddle exp(-2*pi*i*k/L) = post_lo[k%64]*post_hi[k/64] (k <= M/2).
+struct TwiddleTables {
+    float2 *pass_lo = nullptr;
+    float2 *pass_hi = nullptr;
+    float2 *post_lo = nullptr;
+    float2 *post_hi = nullptr;
+    int n_pass_hi = 0;
+    int n_post_hi = 0;
+};
+
+/// Arguments of one F-engine launch: `frames` x `n_station` real FFTs.
+struct FengineArgs {
+    const int8_t *samples;      // frame f of station s: samples + s*station_stride + f*frame_stride
+    size_t station_stride;
+    size_t frame_stride;
+    const uint8_t *mask;        // nullable; bit (mask_bit0+f) of mask + s*mask_station_stride
+    size_t mask_station_stride;
+    int mask_bit0;
+    int n_station;
+    int frames;
+    float2 *y;                  // spectra, y[((size_t)f*n_station + s)*n_freq + k]
+    int *err;
+};
+
+/// Arguments of one X-engine launch over `frames` frames of spectra.
+struct XengineArgs {
+    const float2 *y;            // as FengineArgs::y
+    int n_station;
+    int n_freq;
+    int frames;
+    float2 *acc;                // acc[b*n_freq + c] +=
+    int *err;
+};
+
+// fengine.cu
+corr_status fengine_prepare(int n_freq, TwiddleTables *tw);
+void fengine_release(TwiddleTables *tw);
+corr_status fengine_launch(int n_freq, const TwiddleTables &tw, const FengineArgs &a,
+                           int num_sms, cudaStream_t stream);
+
+// xengine.cu
+corr_status xengine_plain_launch(const XengineArgs &a, int num_sms, cudaStream_t stream);
+corr_status scale_launch(float2 *acc, size_t n, float s, cudaStream_t stream);
+corr_status watchdog_selftest_launch(int *err, long long budget_cycles, cudaStream_t stream);
+
+// xengine_tc.cu
+size_t xengine_tc_workspace_bytes(int n_station, int n_freq);
+corr_status xengine_tc_launch(const XengineArgs &a, bool split, int num_sms,
+                              cudaStream_t stream);
+
+/// An FX plan: everything one device needs to turn int8 frames into added
+/// visibilities, independent of where the frames came from.
+struct FxPlan {
+    int device = 0;
+    int n_station = 0;
+    int n_freq = 0;
+    int n_baseline = 0;
+    int max_frames = 0;   // frames per F/X pass (spectra buffer depth)
+    int xmode = CORR_X_PLAIN_FP32;
+    int num_sms = 0;
+    float2 *d_y = nullptr;
+    int *d_err = nullptr;
+    TwiddleTables tw;
+};
+
+corr_status fxplan_create(int device, int n_station, int n_freq, int max_frames, int xmode,
+                          FxPlan **out);
+void fxplan_destroy(FxPlan *p);
+
+/// F then X over `frames` frames, in passes of at most max_frames.
+corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_stride,
+                              size_t frame_stride, const uint8_t *mask,
+                              size_t mask_station_stride, int mask_bit0, int frames,
+                              float2 *acc, cudaStream_t stream);
+
+/// Read and clear the device watchdog flag (synchronises the device).
+corr_status fxplan_check(FxPlan *p);
+
+/// Host-side validation shared by corr_create and corrx_create.
+corr_status check_geometry(int n_station, int n_freq);
+
+} // namespace corrgb
+
+#endif // CORR_GB300_ENGINE_H

@@ -1,0 +1,203 @@
+// xengine.cu -- plain FP32 X-engine and the row scaling kernel.
+//
+// Replaces corr_kernel (corr-cuda/src/kernels.cu:194-265): for every baseline
+// b = (j,k), j <= k, and channel c,
+//     acc[b][c] += sum_f Y_j[f][c] * conj(Y_k[f][c])
+// with the reference's complex multiply-accumulate convention
+//     re += xr*yr + xi*yi,  im += xi*yr - xr*yi          (kernels.cu:243-245)
+// in FP32.
+//
+// Shape: a CTA owns a tile of 32 channels (lane = channel) and a group of 4x4
+// station blocks (warp = block pair). Spectra for a few frames of every
+// station in the tile are staged in shared memory by a 3-deep cp.async ring;
+// each thread keeps 16 complex accumulators in registers for the whole launch
+// and adds them into the row once at the end. Unlike the reference (one thread
+// per baseline, <= 1024 threads per block) the station-block tiling gives each
+// shared-memory load four multiply-accumulates.
+
+#include <algorithm>
+
+#include "engine.h"
+#include "ptx.cuh"
+
+namespace corrgb {
+namespace {
+
+constexpr int kXch = 32;     // channels per CTA, one per lane
+constexpr int kXfs = 4;      // frames per pipeline stage
+constexpr int kXstages = 3;  // cp.async ring depth
+constexpr int kBlk = 4;      // stations per block
+
+__device__ __forceinline__ void decode_pair(int p, int nb, int *bj, int *bk) {
+    int j = 0;
+    while (p >= nb - j) {
+        p -= nb - j;
+        ++j;
+    }
+    *bj = j;
+    *bk = j + p;
+}
+
+__global__ void __launch_bounds__(1024, 1)
+    xengine_plain_kernel(const float2 *__restrict__ y, int n_station, int npad, int n_freq,
+                         int frames, float2 *__restrict__ acc, int pairs_per_cta,
+                         int n_pairs) {
+    extern __shared__ __align__(16) float2 xs[];   // [stage][frame][npad][32]
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nthreads = blockDim.x;
+    const int c0 = blockIdx.y * kXch;
+    const int nb = npad / kBlk;
+    const int p = blockIdx.x * pairs_per_cta + warp;
+    const bool active = p < n_pairs && warp < pairs_per_cta;
+    int bj = 0, bk = 0;
+    if (active) decode_pair(p, nb, &bj, &bk);
+
+    const int stage_elems = kXfs * npad * kXch;
+    const int chunks = stage_elems / 2;   // 16-byte pieces per stage
+    const int n_stages = (frames + kXfs - 1) / kXfs;
+
+    auto load_stage = [&](int s) {
+        float2 *dst = xs + (s % kXstages) * stage_elems;
+        const int f0 = s * kXfs;
+        for (int q = threadIdx.x; q < chunks; q += nthreads) {
+            const int part = q & 15;                 // 16 pieces of 16 B per row
+            const int row = q >> 4;                  // frame*npad + station
+            const int fi = row / npad;
+            const int st = row - fi * npad;
+            const int f = f0 + fi;
+            const bool ok = (st < n_station) && (f < frames);
+            const float2 *src =
+                ok ? y + (static_cast<size_t>(f) * n_station + st) * n_freq + c0 + part * 2 : y;
+            cp_async16(dst + row * kXch + part * 2, src, ok ? 16u : 0u);
+        }
+    };
+
+    float2 a[kBlk][kBlk];
+#pragma unroll
+    for (int i = 0; i < kBlk; ++i)
+#pragma unroll
+        for (int l = 0; l < kBlk; ++l) a[i][l] = make_float2(0.f, 0.f);
+
+#pragma unroll
+    for (int s = 0; s < kXstages - 1; ++s) {
+        if (s < n_stages) load_stage(s);
+        cp_async_commit();
+    }
+    for (int s = 0; s < n_stages; ++s) {
+        cp_async_wait<kXstages - 2>();
+        __syncthreads();
+        if (s + kXstages - 1 < n_stages) load_stage(s + kXstages - 1);
+        cp_async_commit();
+        if (active) {
+            const float2 *st = xs + (s % kXstages) * stage_elems;
+#pragma unroll
+            for (int fi = 0; fi < kXfs; ++fi) {
+                const float2 *fr = st + fi * npad * kXch + lane;
+                float2 xj[kBlk], xk[kBlk];
+#pragma unroll
+                for (int i = 0; i < kBlk; ++i) {
+                    xj[i] = fr[(bj * kBlk + i) * kXch];
+                    xk[i] = fr[(bk * kBlk + i) * kXch];
+                }
+#pragma unroll
+                for (int i = 0; i < kBlk; ++i)
+#pragma unroll
+                    for (int l = 0; l < kBlk; ++l) {
+                        a[i][l].x += xj[i].x * xk[l].x + xj[i].y * xk[l].y;
+                        a[i][l].y += xj[i].y * xk[l].x - xj[i].x * xk[l].y;
+                    }
+            }
+        }
+    }
+    cp_async_wait<0>();
+
+    if (!active) return;
+    const int c = c0 + lane;
+#pragma unroll
+    for (int i = 0; i < kBlk; ++i) {
+        const int j = bj * kBlk + i;
+#pragma unroll
+        for (int l = 0; l < kBlk; ++l) {
+            const int k = bk * kBlk + l;
+            if (j <= k && k < n_station) {
+                const int b = j * n_station - j * (j - 1) / 2 + (k - j);
+                float2 *dst = acc + static_cast<size_t>(b) * n_freq + c;
+                float2 v = *dst;
+                v.x += a[i][l].x;
+                v.y += a[i][l].y;
+                *dst = v;
+            }
+        }
+    }
+}
+
+__global__ void scale_kernel(float2 *__restrict__ acc, size_t n, float s) {
+    const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+    for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += stride) {
+        float2 v = acc[i];
+        v.x *= s;
+        v.y *= s;
+        acc[i] = v;
+    }
+}
+
+// One thread waits on an mbarrier whose phase never completes (nothing arrives
+// on it), with a caller-chosen budget; the bounded wait gives up and records
+// kErrSelftestTimeout. The barrier is then retired by arriving on it so the CTA
+// exits with nothing pending.
+__global__ void watchdog_selftest_kernel(int *err, long long budget) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x != 0) return;
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    const long long t0 = clock64();
+    bool done = false;
+    while (!(done = mbar_try_wait(&bar, 0u))) {
+        if (clock64() - t0 > budget) break;
+    }
+    if (!done) atomicExch(err, kErrSelftestTimeout);
+    mbar_arrive(&bar);
+}
+
+} // namespace
+
+corr_status watchdog_selftest_launch(int *err, long long budget_cycles, cudaStream_t stream) {
+    watchdog_selftest_kernel<<<1, 32, 0, stream>>>(err, budget_cycles);
+    return cuda_check(cudaGetLastError(), "watchdog_selftest_kernel launch");
+}
+
+corr_status xengine_plain_launch(const XengineArgs &a, int num_sms, cudaStream_t stream) {
+    (void)num_sms;
+    if (a.frames <= 0) return CORR_OK;
+    const int npad = (a.n_station + kBlk - 1) / kBlk * kBlk;
+    const int nb = npad / kBlk;
+    const int n_pairs = nb * (nb + 1) / 2;
+    const int groups = (n_pairs + 31) / 32;
+    const int per_cta = (n_pairs + groups - 1) / groups;
+    const size_t smem = static_cast<size_t>(kXstages) * kXfs * npad * kXch * sizeof(float2);
+    static bool configured = false;
+    if (!configured) {
+        corr_status st = cuda_check(
+            cudaFuncSetAttribute(xengine_plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 227 * 1024),
+            "cudaFuncSetAttribute(xengine_plain)");
+        if (st != CORR_OK) return st;
+        configured = true;
+    }
+    dim3 grid(groups, a.n_freq / kXch);
+    xengine_plain_kernel<<<grid, per_cta * 32, smem, stream>>>(
+        a.y, a.n_station, npad, a.n_freq, a.frames, a.acc, per_cta, n_pairs);
+    return cuda_check(cudaGetLastError(), "xengine_plain_kernel launch");
+}
+
+corr_status scale_launch(float2 *acc, size_t n, float s, cudaStream_t stream) {
+    if (n == 0) return CORR_OK;
+    size_t blocks = (n + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    scale_kernel<<<static_cast<unsigned>(blocks), 256, 0, stream>>>(acc, n, s);
+    return cuda_check(cudaGetLastError(), "scale_kernel launch");
+}
+
+} // namespace corrgb

@@ -1,0 +1,433 @@
+"""Benchmark: fused F+X GSample/s on one GB300 (or N replicas), one JSON line.
+
+Workload (default): 24 inputs, n_freq 16384 (32768-sample frames), 4096 frames
+per integration -- the precision workload the throughput target is quoted on.
+A step is one integration: zero the accumulator, F-engine + X-engine over all
+4096 frames (passes of 256 frames), scale by 1/4096. Inputs (3.2 GB of int8)
+are generated in HBM before timing and are larger than L2, so no flush is needed.
+
+  value      : device-resident throughput, int8 samples in per second (GS/s)
+  e2e        : the same integration through the C ABI (corr_row_accumulate from
+               the pinned staging ring, H2D inside the timed region, fetch to host)
+  roofline   : the dominant kernel's achieved algorithmic bytes/s vs measured HBM
+  cpu_baseline: the numpy float64 oracle (the reference's gen_golden.py
+               formulation) on a bounded sample, on this host's cores
+
+--impl reference runs the reference's CPU formulation of the path (the oracle
+port, multi-process over all host cores) on the same workload and metric.
+"""
+
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+PKG_NAME = "21cma_abf_correlator_gb300"
+METRIC = "fused F+X GSample/s"
+MAX_FRAMES = 256
+
+
+def peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-i", str(self.gpu), "-lms", "100"], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_oracle_sample(w, frames: int, seed_offset: int = 0):
+    synth = importlib.import_module(PKG_NAME + ".synth")
+    x, mask = synth.generate_numpy(w, frames, seed_offset)
+    present = None if mask is None else synth.unpack_mask(mask, frames)
+    return x, present
+
+
+def _oracle_worker(args):
+    """Generate a sample (untimed), then time the oracle on it."""
+    name, frames, seed_offset = args
+    synth = importlib.import_module(PKG_NAME + ".synth")
+    oracle = importlib.import_module("oracle.corr_oracle")
+    w = synth.WORKLOADS[name]
+    x, present = cpu_oracle_sample(w, frames, seed_offset)
+    t0 = time.perf_counter()
+    oracle.correlate(x, present)
+    return time.perf_counter() - t0
+
+
+def time_cpu_oracle(w, target_s: float, processes: int) -> dict:
+    """Time the float64 oracle on frames of this workload, spread over `processes`."""
+    L = w.fft_len
+    # calibrate on one frame in this process
+    probe = _oracle_worker((w.name, 1, 0))
+    per_frame = max(probe, 1e-4)
+    frames_per_proc = max(1, int(target_s / per_frame / 1.2))
+    frames_per_proc = min(frames_per_proc, 512)
+    if processes <= 1:
+        wall = _oracle_worker((w.name, frames_per_proc, 1))
+    else:
+        import multiprocessing as mp
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(processes) as pool:
+            pool.map(_oracle_worker, [(w.name, 1, 100 + i) for i in range(processes)])  # warm
+            # workers run concurrently; the slowest one's compute time is the wall
+            wall = max(pool.map(_oracle_worker, [(w.name, frames_per_proc, 200 + i)
+                                                 for i in range(processes)]))
+    samples = w.n_station * frames_per_proc * processes * L
+    return {"value": samples / wall / 1e9, "unit": "GSample/s", "cores": processes,
+            "sample": f"{frames_per_proc * processes} frames x {w.n_station} inputs x {L} samples "
+                      f"({w.name}), numpy float64 rfft + per-baseline sum, "
+                      f"{processes} process(es), {wall:.1f} s wall"}
+
+
+def run_reference(args) -> None:
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    synth = importlib.import_module(PKG_NAME + ".synth")
+    w = synth.WORKLOADS[args.workload]
+    procs = os.cpu_count() or 1
+    vals = []
+    for _ in range(args.warmup):
+        time_cpu_oracle(w, 3.0, procs)
+    for _ in range(args.steps):
+        vals.append(time_cpu_oracle(w, args.cpu_seconds, procs))
+    v = statistics.median([x["value"] for x in vals])
+    frames_step = w.frames
+    samples_step = w.n_station * frames_step * w.fft_len
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "GSample/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": samples_step / (v * 1e9) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w.name, "n_station": w.n_station, "n_freq": w.n_freq,
+                   "frames_per_integration": w.frames, "path": "numpy float64 oracle "
+                   "(reference corr-cuda/tests/gen_golden.py formulation) on host cores"},
+        "cpu_baseline": {"value": v, "unit": "GSample/s", "cores": procs, "kind": "port",
+                         "sample": vals[-1]["sample"]},
+        "e2e": {"value": v, "unit": "GSample/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="precision-24in-nf16384")
+    ap.add_argument("--xmode", default="auto", choices=["auto", "plain", "tc", "tc_split"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    build = importlib.import_module(PKG_NAME + ".build")
+    if rank == 0:
+        build.build()
+    if world > 1:
+        torch.distributed.barrier()
+    pkg = importlib.import_module(PKG_NAME)
+    synth = importlib.import_module(PKG_NAME + ".synth")
+    abi = pkg.abi
+    w = synth.WORKLOADS[args.workload]
+    N, nf, F, L = w.n_station, w.n_freq, w.frames, w.fft_len
+    B = w.n_baseline
+
+    modes = {"plain": abi.CORR_X_PLAIN_FP32, "tc": abi.CORR_X_TC_FP16,
+             "tc_split": abi.CORR_X_TC_FP16_SPLIT}
+    if args.xmode == "auto":
+        candidates = ["tc_split", "plain"]
+    else:
+        candidates = [args.xmode]
+
+    x, mask = synth.generate_torch(w, F, seed_offset=rank)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    samples_step = N * F * L
+
+    def make_step(eng, acc):
+        def step():
+            acc.zero_()
+            eng.accumulate(x, F, acc, mask=mask, stream=stream)
+            eng.scale(acc, F, stream=stream)
+        return step
+
+    results = {}
+    engines = {}
+    for name in candidates:
+        try:
+            eng = pkg.FxEngine(N, nf, MAX_FRAMES, xmode=modes[name])
+            acc = eng.new_acc()
+            step = make_step(eng, acc)
+            step()
+            torch.cuda.synchronize()
+            eng.check()
+        except pkg.CorrError as e:
+            if e.status == abi.CORR_ERR_NOT_IMPL:
+                continue
+            raise
+        engines[name] = (eng, acc, step)
+    if not engines:
+        raise SystemExit("no X-engine available")
+
+    def time_steps(step, k, w_):
+        for _ in range(w_):
+            step()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        return e0.elapsed_time(e1) / k
+
+    # pick the headline path: the fastest available X-engine
+    per_path = {}
+    for name, (eng, acc, step) in engines.items():
+        per_path[name] = time_steps(step, 2, 1)
+    best = min(per_path, key=per_path.get)
+    eng, acc, step = engines[best]
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    ms = time_steps(step, args.steps, args.warmup)
+    clocks = sampler.stop()
+    eng.check()
+
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = samples_step * world / (ms * 1e-3) / 1e9
+
+    paths = {}
+    for name, (e_, a_, s_) in engines.items():
+        m = ms if name == best else time_steps(s_, max(2, args.steps // 2), 1)
+        paths[name] = {"value": samples_step / (m * 1e-3) / 1e9, "ms_per_step": m}
+
+    # per-kernel times: one pass of MAX_FRAMES frames through each kernel alone
+    hbm_peak, _, peak_kind = peaks()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    reps = 8
+    for _ in range(2):
+        abi.check(eng.lib.corrx_run_fengine(eng.h, x.data_ptr(), x.stride(0), x.stride(1),
+                                            mask.data_ptr() if mask is not None else None,
+                                            mask.stride(0) if mask is not None else 0, 0,
+                                            MAX_FRAMES, stream.cuda_stream), "fengine")
+        abi.check(eng.lib.corrx_run_xengine(eng.h, MAX_FRAMES, acc.data_ptr(),
+                                            stream.cuda_stream), "xengine")
+    torch.cuda.synchronize()
+    t_f = t_x = 0.0
+    for r in range(reps):
+        f0 = (r * MAX_FRAMES) % (F - MAX_FRAMES + 1)
+        base = x.data_ptr() + f0 * x.stride(1)
+        ev[0].record(stream)
+        abi.check(eng.lib.corrx_run_fengine(eng.h, base, x.stride(0), x.stride(1),
+                                            mask.data_ptr() if mask is not None else None,
+                                            mask.stride(0) if mask is not None else 0, f0,
+                                            MAX_FRAMES, stream.cuda_stream), "fengine")
+        ev[1].record(stream)
+        abi.check(eng.lib.corrx_run_xengine(eng.h, MAX_FRAMES, acc.data_ptr(),
+                                            stream.cuda_stream), "xengine")
+        ev[2].record(stream)
+        torch.cuda.synchronize()
+        t_f += ev[0].elapsed_time(ev[1])
+        t_x += ev[1].elapsed_time(ev[2])
+    t_f /= reps
+    t_x /= reps
+    mb = synth.mask_bytes(F) if mask is not None else 0
+    f_bytes = N * MAX_FRAMES * L + N * MAX_FRAMES * nf * 8 + (N * mb * MAX_FRAMES // F)
+    x_bytes = N * MAX_FRAMES * nf * 8 + 2 * B * nf * 8
+    kernels = {
+        "fengine": {"ms_per_launch": t_f, "alg_bytes": f_bytes,
+                    "achieved_gbs": f_bytes / (t_f * 1e-3) / 1e9},
+        "xengine_" + best: {"ms_per_launch": t_x, "alg_bytes": x_bytes,
+                            "achieved_gbs": x_bytes / (t_x * 1e-3) / 1e9,
+                            "alg_tflops": 8.0 * B * nf * MAX_FRAMES / (t_x * 1e-3) / 1e12},
+    }
+    dom = "fengine" if t_f >= t_x else "xengine_" + best
+    dk = kernels[dom]
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": dk["achieved_gbs"],
+                "peak": hbm_peak, "unit": "GB/s", "frac": dk["achieved_gbs"] / hbm_peak,
+                "peak_kind": peak_kind, "traffic": None,
+                "alg_bytes_per_launch": dk["alg_bytes"], "frames_per_launch": MAX_FRAMES}
+
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        e2e = run_e2e(pkg, w, x, mask, modes[best], args, torch)
+
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        cpu = time_cpu_oracle(w, args.cpu_seconds, 1)
+        cpu["kind"] = "port"
+
+    passes = math.ceil(F / MAX_FRAMES)
+    launches_per_step = 2 * passes + 1
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "GSample/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int8 in, f32 FFT, " + ("f32 X" if best == "plain" else "f16 tensor X"),
+            "data": "synthetic (seeded Gaussian + common signal, delays; generated in HBM)",
+            "config": {"workload": w.name, "n_station": N, "n_freq": nf,
+                       "frames_per_integration": F, "baselines": B, "xengine": best,
+                       "frames_per_pass": MAX_FRAMES, "parallelism": f"replicas x{world}",
+                       "l2": f"inputs {N * F * L / 1e9:.2f} GB per step > L2; no flush"},
+            "paths": paths, "kernels": kernels, "roofline": roofline,
+            "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
+            "gpu_launches": launches_per_step * args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_e2e(pkg, w, x, mask, xmode, args, torch) -> dict:
+    """The integration through the C ABI: staging -> H2D -> F+X -> row -> host."""
+    fps, block_slots = 256, 4
+    N, L, F = w.n_station, w.fft_len, w.frames
+    cfg = pkg.make_config(N, w.n_freq, fps, fps, block_slots, 1)
+    c = pkg.Correlator(cfg)
+    c.set_xengine(xmode)
+    # fill the ring once from the device-resident inputs (receive side's job)
+    host = x[:, : fps * block_slots].cpu().numpy()
+    for g in range(N):
+        v = c.staging(g)
+        v.samples[:] = host[g].reshape(block_slots, fps, L)
+    out = np.empty(c.fetch_bytes() // 8, dtype=np.complex64)
+    import ctypes as C
+    pinned = C.c_void_p()
+    pkg.abi.check(c.lib.corr_host_alloc(out.nbytes, C.byref(pinned)), "corr_host_alloc")
+    rows = C.c_int32()
+    seq = [0]
+
+    def integration():
+        for f0 in range(0, F, fps):
+            s = seq[0]
+            if s >= block_slots:
+                c.row_slot_free(s - block_slots)
+            for g in range(N):
+                c.staging(g).mask[s % block_slots, :] = 0xFF
+            c.row_accumulate(s, min(fps, F - f0))
+            seq[0] += 1
+        c.row_end(F)
+        pkg.abi.check(c.lib.corr_rows_fetch(c.ctx, pinned, out.nbytes, C.byref(rows)),
+                      "corr_rows_fetch")
+
+    for _ in range(2):
+        integration()
+    t0 = time.perf_counter()
+    k = max(2, args.steps // 2)
+    for _ in range(k):
+        integration()
+    dt = (time.perf_counter() - t0) / k
+    for s in range(seq[0] - 1, max(seq[0] - block_slots, 0) - 1, -1):
+        c.row_slot_free(s)
+    c.lib.corr_host_free(pinned)
+    c.close()
+    mb = (fps + 7) // 8
+    h2d = N * F * L + N * mb * (F // fps)
+    d2h = w.n_baseline * w.n_freq * 8
+    return {"value": N * F * L / dt / 1e9, "unit": "GSample/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "ms_per_step": dt * 1e3, "steps": k,
+            "path": "corr_row_accumulate/row_end/rows_fetch from pinned staging"}
+
+
+if __name__ == "__main__":
+    main()

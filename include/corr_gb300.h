@@ -1,0 +1,94 @@
+/*
+ * corr_gb300.h -- extensions of the GB300 engine beyond the reference ABI.
+ *
+ * None of these has a counterpart in the reference's public header; they expose
+ * what the reference keeps internal (corr-cuda/src/gpu_internal.h, the per-chunk
+ * work of gpu_accumulate at corr-cuda/src/kernels.cu:684-857) so that callers
+ * holding data already in device memory -- benchmarks, a batching front end, a
+ * multi-integration replay -- can drive the F- and X-engines without going
+ * through the pinned staging ring. The same kernels run behind corr_cuda.h.
+ *
+ * All device pointers are plain CUDA device addresses; `stream` is a
+ * cudaStream_t passed as void* (NULL = the legacy default stream).
+ */
+
+#ifndef CORR_GB300_H
+#define CORR_GB300_H
+
+#include "corr_cuda.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* X-engine forms. */
+#define CORR_X_PLAIN_FP32    0 /* FP32 SIMT complex multiply-accumulate (default)     */
+#define CORR_X_TC_FP16       1 /* tcgen05: FP16 spectra, per-channel power-of-two
+                                  scale, FP32 accumulation in tensor memory          */
+#define CORR_X_TC_FP16_SPLIT 2 /* as CORR_X_TC_FP16 with a hi/lo split product that
+                                  recovers about 22 bits of the spectra               */
+
+/* Select the X-engine of an ABI context. Allowed only while no row holds data
+   (after corr_create, or right after a fetch). */
+corr_status corr_set_xengine(void *ctx, int32_t mode);
+
+typedef struct corrx_params {
+    uint32_t struct_size; /* sizeof(corrx_params)                                 */
+    int32_t  n_station;   /* 1..44                                                */
+    int32_t  n_freq;      /* power of two in [512, 16384]                         */
+    int32_t  max_frames;  /* frames per F/X pass; sizes the spectra buffer
+                             (max_frames*n_station*n_freq*8 bytes)               */
+    int32_t  xmode;       /* CORR_X_*                                             */
+    int32_t  device_id;   /* CUDA ordinal                                         */
+} corrx_params;
+
+/* Create / destroy a device-resident engine (spectra buffer, twiddle tables,
+   watchdog flag). */
+corr_status corrx_create(const corrx_params *p, void **out_eng);
+corr_status corrx_destroy(void *eng);
+
+/*
+ * acc[b*n_freq + c] += sum over frames f < `frames` of Y_j[f][c]*conj(Y_k[f][c])
+ * for every baseline b = (j,k), j <= k, in corr_baseline_pairs() order.
+ *
+ * Frame f of station s is 2*n_freq int8 samples at
+ *   d_samples + s*station_stride + f*frame_stride            (16-byte aligned)
+ * If d_mask is not NULL, frame f of station s is treated as all zeros unless bit
+ * (mask_bit0 + f) of the bit string at d_mask + s*mask_station_stride is set
+ * (LSB first), exactly as the staging validity mask is read.
+ * d_acc holds n_baseline*n_freq complex64 (FP32 re, im) and must not alias.
+ */
+corr_status corrx_accumulate(void *eng, const int8_t *d_samples, size_t station_stride,
+                             size_t frame_stride, const uint8_t *d_mask,
+                             size_t mask_station_stride, int32_t mask_bit0, int32_t frames,
+                             void *d_acc, void *stream);
+
+/* d_acc *= 1.0f/(float)frames over n_baseline*n_freq complex values. */
+corr_status corrx_scale(void *eng, void *d_acc, uint64_t frames, void *stream);
+
+/* Synchronise the engine's device and report a tripped device watchdog
+   (CORR_ERR_INTERNAL) or a CUDA error. */
+corr_status corrx_check(void *eng);
+
+/* The two halves of corrx_accumulate, for timing and profiling each kernel on
+   its own. corrx_run_fengine transforms `frames` (<= max_frames) frames into the
+   engine's spectra buffer; corrx_run_xengine correlates the first `frames`
+   frames of that buffer into d_acc. */
+corr_status corrx_run_fengine(void *eng, const int8_t *d_samples, size_t station_stride,
+                              size_t frame_stride, const uint8_t *d_mask,
+                              size_t mask_station_stride, int32_t mask_bit0, int32_t frames,
+                              void *stream);
+corr_status corrx_run_xengine(void *eng, int32_t frames, void *d_acc, void *stream);
+
+/* Watchdog self-test: launches one block that waits on an mbarrier nothing will
+   ever complete, with a budget of `budget_cycles` clock cycles. The wait runs
+   out, the kernel records the timeout in the engine's watchdog flag and returns;
+   corrx_check() then reports CORR_ERR_INTERNAL and clears the flag. Exists so
+   the timeout path of every bounded wait can be exercised without hanging a GPU. */
+corr_status corrx_selftest_watchdog(void *eng, int64_t budget_cycles, void *stream);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* CORR_GB300_H */
