@@ -141,11 +141,13 @@ corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_s
         fa.n_station = p->n_station;
         fa.frames = ft;
         fa.y = p->d_y;
+        fa.y_frames = p->max_frames;
         fa.err = p->d_err;
         corr_status st = fengine_launch(p->n_freq, p->tw, fa, p->num_sms, stream);
         if (st != CORR_OK) return st;
         XengineArgs xa{};
         xa.y = p->d_y;
+        xa.y_frames = p->max_frames;
         xa.n_station = p->n_station;
         xa.n_freq = p->n_freq;
         xa.frames = ft;
@@ -259,6 +261,7 @@ extern "C" corr_status corrx_run_fengine(void *eng, const int8_t *d_samples,
     fa.n_station = p->n_station;
     fa.frames = frames;
     fa.y = p->d_y;
+    fa.y_frames = p->max_frames;
     fa.err = p->d_err;
     return fengine_launch(p->n_freq, p->tw, fa, p->num_sms, static_cast<cudaStream_t>(stream));
 }
@@ -273,6 +276,7 @@ extern "C" corr_status corrx_run_xengine(void *eng, int32_t frames, void *d_acc,
     if (st != CORR_OK) return st;
     XengineArgs xa{};
     xa.y = p->d_y;
+    xa.y_frames = p->max_frames;
     xa.n_station = p->n_station;
     xa.n_freq = p->n_freq;
     xa.frames = frames;

@@ -40,9 +40,9 @@ enum : int {
 ///   pass_lo[u]  = exp(-2*pi*i*u/M)        u in [0, 64)
 ///   pass_hi[u]  = exp(-2*pi*i*64*u/M)     u in [0, M/64)
 ///   post_lo[k]  = exp(-pi*i*k/M)          k in [0, 64)
-///   post_hi[k]  = exp(-pi*i*64*k/M)       k in [0, M/128 + 1)
+///   post_hi[k]  = exp(-pi*i*64*k/M)       k in [0, M/64)
 /// so exp(-2*pi*i*u/M) = pass_lo[u%64]*pass_hi[u/64] (u < M) and the real-FFT
-/// split twiddle exp(-2*pi*i*k/L) = post_lo[k%64]*post_hi[k/64] (k <= M/2).
+/// split twiddle exp(-2*pi*i*k/L) = post_lo[k%64]*post_hi[k/64] (k < M).
 struct TwiddleTables {
     float2 *pass_lo = nullptr;
     float2 *pass_hi = nullptr;
@@ -51,6 +51,17 @@ struct TwiddleTables {
     int n_pass_hi = 0;
     int n_post_hi = 0;
 };
+
+/// Spectra layout shared by the F- and X-engines: channel-tiled,
+///   y[((c / kYTile) * y_frames + f) * n_station + s) * kYTile + c % kYTile]
+/// so one channel tile of every station over consecutive frames is a single
+/// contiguous block (what an X-engine CTA streams with one bulk copy per stage).
+constexpr int kYTile = 4;
+
+__host__ __device__ inline size_t y_index(int c, int f, int s, int n_station, int y_frames) {
+    return ((static_cast<size_t>(c / kYTile) * y_frames + f) * n_station + s) * kYTile +
+           (c % kYTile);
+}
 
 /// Arguments of one F-engine launch: `frames` x `n_station` real FFTs.
 struct FengineArgs {
@@ -62,13 +73,15 @@ struct FengineArgs {
     int mask_bit0;
     int n_station;
     int frames;
-    float2 *y;                  // spectra, y[((size_t)f*n_station + s)*n_freq + k]
+    float2 *y;                  // spectra, channel-tiled (y_index)
+    int y_frames;               // frames the spectra buffer holds
     int *err;
 };
 
 /// Arguments of one X-engine launch over `frames` frames of spectra.
 struct XengineArgs {
     const float2 *y;            // as FengineArgs::y
+    int y_frames;               // frames the spectra buffer holds (>= frames)
     int n_station;
     int n_freq;
     int frames;

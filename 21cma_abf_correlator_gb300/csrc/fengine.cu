@@ -18,9 +18,10 @@
 //     bins 0..M-1 are written, the Nyquist bin M is dropped and nothing is
 //     normalised (reference semantics, HANDOFF.md:583-602).
 //
-// Output layout: y[(frame*n_station + station)*M + k], complex64. One row per
-// (frame, station), channel-contiguous, so the X-engines read a channel tile of
-// every station of a frame as n_station coalesced segments.
+// Output layout: complex64, channel-tiled (engine.h, y_index): bin k of
+// (frame f, station s) lands in tile k/4 at ((k/4)*y_frames + f)*n_station + s,
+// slot k%4. A warp's 32 consecutive bins are eight whole 32-byte sectors, and
+// an X-engine CTA then reads its tiles over many frames as contiguous blocks.
 
 #include <cmath>
 #include <vector>
@@ -31,13 +32,41 @@
 namespace corrgb {
 namespace {
 
-// Shared-memory index padding: one float2 of padding per 16, which makes the
-// stride-16 scatter of the first Stockham pass conflict-free.
-__device__ __forceinline__ int padi(int i) { return i + (i >> 4); }
-
 // ---------------------------------------------------------------------------
 // Small DFTs in registers, forward sign (exp(-2*pi*i*n*k/R)), natural order.
+// All constant twiddles are 32nd roots of unity.
 // ---------------------------------------------------------------------------
+
+// cos(2*pi*m/32) and sin(2*pi*m/32) for m in [0, 32), built from the first octant.
+__host__ __device__ constexpr float cos32_q(int r) {
+    return r == 0 ? 1.0f
+         : r == 1 ? 0.98078528040323044913f
+         : r == 2 ? 0.92387953251128675613f
+         : r == 3 ? 0.83146961230254523708f
+         : r == 4 ? 0.70710678118654752440f
+         : r == 5 ? 0.55557023301960222474f
+         : r == 6 ? 0.38268343236508977173f
+         : r == 7 ? 0.19509032201612826785f
+                  : 0.0f;
+}
+__host__ __device__ constexpr float cos32(int m) {
+    return (m & 31) < 8    ? cos32_q(m & 31)
+         : (m & 31) < 16 ? -cos32_q(16 - (m & 31))
+         : (m & 31) < 24 ? -cos32_q((m & 31) - 16)
+                         : cos32_q(32 - (m & 31));
+}
+__host__ __device__ constexpr float sin32(int m) { return cos32(m - 8); }
+
+// a * exp(-2*pi*i*m/32); m is a compile-time constant after unrolling.
+__device__ __forceinline__ float2 mul_w32(float2 a, int m) {
+    m &= 31;
+    if (m == 0) return a;
+    if (m == 8) return make_float2(a.y, -a.x);
+    if (m == 16) return make_float2(-a.x, -a.y);
+    if (m == 24) return make_float2(-a.y, a.x);
+    const float c = cos32(m), s = sin32(m);
+    return make_float2(fmaf(a.x, c, a.y * s), fmaf(a.y, c, -a.x * s));
+}
 
 template <int R>
 struct Dft;
@@ -63,61 +92,28 @@ struct Dft<4> {
     }
 };
 
-// cos(pi/4), cos(pi/8), sin(pi/8)
-#define CORR_H 0.70710678118654752440f
-#define CORR_C1 0.92387953251128675613f
-#define CORR_S1 0.38268343236508977173f
-
-template <>
-struct Dft<8> {
+// R = 4 x (R/4): n = (R/4)*n1 + n2, k = k1 + 4*k2.
+template <int R>
+struct Dft {
+    static_assert(R == 8 || R == 16 || R == 32, "radix");
+    static constexpr int R2 = R / 4;
     static __device__ __forceinline__ void run(float2 *v) {
-        float2 e[4] = {v[0], v[2], v[4], v[6]};
-        float2 o[4] = {v[1], v[3], v[5], v[7]};
-        Dft<4>::run(e);
-        Dft<4>::run(o);
-        // o[k] *= exp(-i*pi*k/4)
-        o[1] = make_float2(CORR_H * (o[1].x + o[1].y), CORR_H * (o[1].y - o[1].x));
-        o[2] = make_float2(o[2].y, -o[2].x);
-        o[3] = make_float2(CORR_H * (o[3].y - o[3].x), -CORR_H * (o[3].x + o[3].y));
+        float2 b[R2][4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            v[k] = cadd(e[k], o[k]);
-            v[k + 4] = csub(e[k], o[k]);
-        }
-    }
-};
-
-template <>
-struct Dft<16> {
-    // 16 = 4 x 4: n = 4*n1 + n2, k = k1 + 4*k2.
-    static __device__ __forceinline__ void run(float2 *v) {
-        float2 b[4][4];
-#pragma unroll
-        for (int n2 = 0; n2 < 4; ++n2) {
-            float2 t[4] = {v[n2], v[4 + n2], v[8 + n2], v[12 + n2]};
+        for (int n2 = 0; n2 < R2; ++n2) {
+            float2 t[4] = {v[n2], v[R2 + n2], v[2 * R2 + n2], v[3 * R2 + n2]};
             Dft<4>::run(t);
 #pragma unroll
-            for (int k1 = 0; k1 < 4; ++k1) b[n2][k1] = t[k1];
+            for (int k1 = 0; k1 < 4; ++k1) b[n2][k1] = mul_w32(t[k1], n2 * k1 * (32 / R));
         }
-        // b[n2][k1] *= exp(-2*pi*i*n2*k1/16)
-        const float2 w1 = make_float2(CORR_C1, -CORR_S1);
-        const float2 w3 = make_float2(CORR_S1, -CORR_C1);
-        const float2 w9 = make_float2(-CORR_C1, CORR_S1);
-        b[1][1] = cmul(b[1][1], w1);
-        b[1][2] = make_float2(CORR_H * (b[1][2].x + b[1][2].y), CORR_H * (b[1][2].y - b[1][2].x));
-        b[1][3] = cmul(b[1][3], w3);
-        b[2][1] = make_float2(CORR_H * (b[2][1].x + b[2][1].y), CORR_H * (b[2][1].y - b[2][1].x));
-        b[2][2] = make_float2(b[2][2].y, -b[2][2].x);
-        b[2][3] = make_float2(CORR_H * (b[2][3].y - b[2][3].x), -CORR_H * (b[2][3].x + b[2][3].y));
-        b[3][1] = cmul(b[3][1], w3);
-        b[3][2] = make_float2(CORR_H * (b[3][2].y - b[3][2].x), -CORR_H * (b[3][2].x + b[3][2].y));
-        b[3][3] = cmul(b[3][3], w9);
 #pragma unroll
         for (int k1 = 0; k1 < 4; ++k1) {
-            float2 t[4] = {b[0][k1], b[1][k1], b[2][k1], b[3][k1]};
-            Dft<4>::run(t);
+            float2 t[R2];
 #pragma unroll
-            for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = t[k2];
+            for (int n2 = 0; n2 < R2; ++n2) t[n2] = b[n2][k1];
+            Dft<R2>::run(t);
+#pragma unroll
+            for (int k2 = 0; k2 < R2; ++k2) v[k1 + 4 * k2] = t[k2];
         }
     }
 };
@@ -127,51 +123,93 @@ __device__ __forceinline__ float2 tw_pass(const float2 *lo, const float2 *hi, in
     return cmul(lo[u & 63], hi[u >> 6]);
 }
 
-// v[r] *= w^r with w = exp(-2*pi*i*u/M). w, w^4 and w^8 are read from the
-// table; the other powers are at most two products away from those.
+// v[r] *= w^r with w = exp(-2*pi*i*u/M), u*R < M. w, w^4, w^8 and w^16 come
+// from the table; every other power is at most three products from those.
 template <int R>
 __device__ __forceinline__ void apply_twiddles(float2 *v, int u, const float2 *lo,
                                                const float2 *hi) {
-    const float2 w1 = tw_pass(lo, hi, u);
-    if constexpr (R == 2) {
-        v[1] = cmul(v[1], w1);
-    } else {
-        const float2 w2 = cmul(w1, w1);
-        const float2 w3 = cmul(w2, w1);
-        v[1] = cmul(v[1], w1);
-        v[2] = cmul(v[2], w2);
-        v[3] = cmul(v[3], w3);
-        if constexpr (R >= 8) {
-            const float2 w4 = tw_pass(lo, hi, 4 * u);
-            v[4] = cmul(v[4], w4);
-            v[5] = cmul(v[5], cmul(w4, w1));
-            v[6] = cmul(v[6], cmul(w4, w2));
-            v[7] = cmul(v[7], cmul(w4, w3));
-            if constexpr (R == 16) {
-                const float2 w8 = tw_pass(lo, hi, 8 * u);
-                const float2 w12 = cmul(w8, w4);
-                v[8] = cmul(v[8], w8);
-                v[9] = cmul(v[9], cmul(w8, w1));
-                v[10] = cmul(v[10], cmul(w8, w2));
-                v[11] = cmul(v[11], cmul(w8, w3));
-                v[12] = cmul(v[12], w12);
-                v[13] = cmul(v[13], cmul(w12, w1));
-                v[14] = cmul(v[14], cmul(w12, w2));
-                v[15] = cmul(v[15], cmul(w12, w3));
-            }
-        }
+    float2 w[R];
+    w[1] = tw_pass(lo, hi, u);
+    if constexpr (R >= 4) {
+        w[2] = cmul(w[1], w[1]);
+        w[3] = cmul(w[2], w[1]);
     }
+    if constexpr (R >= 8) {
+        w[4] = tw_pass(lo, hi, 4 * u);
+#pragma unroll
+        for (int r = 5; r < 8; ++r) w[r] = cmul(w[4], w[r - 4]);
+    }
+    if constexpr (R >= 16) {
+        w[8] = tw_pass(lo, hi, 8 * u);
+#pragma unroll
+        for (int r = 9; r < 16; ++r) w[r] = cmul(w[8], w[r - 8]);
+    }
+    if constexpr (R >= 32) {
+        w[16] = tw_pass(lo, hi, 16 * u);
+#pragma unroll
+        for (int r = 17; r < 32; ++r) w[r] = cmul(w[16], w[r - 16]);
+    }
+#pragma unroll
+    for (int r = 1; r < R; ++r) v[r] = cmul(v[r], w[r]);
 }
 
-// One Stockham pass of radix R over M points with sub-transform size NS:
+// Radix plan per transform length M = 2^LOGM: three passes R0 x R1 x R2 = M,
+// P = 2*R2 points per thread, T = M/P threads. The last pass (radix R2) is
+// fused with the real-FFT split: thread t owns butterflies t and J - t
+// (J = M/R2), so Z[k] and Z[M-k] meet in its registers.
+template <int LOGM>
+struct FePlan;
+template <> struct FePlan<14> { static constexpr int R0 = 32, R1 = 32, R2 = 16; };
+template <> struct FePlan<13> { static constexpr int R0 = 32, R1 = 16, R2 = 16; };
+template <> struct FePlan<12> { static constexpr int R0 = 16, R1 = 16, R2 = 16; };
+template <> struct FePlan<11> { static constexpr int R0 = 16, R1 = 8, R2 = 16; };
+template <> struct FePlan<10> { static constexpr int R0 = 16, R1 = 8, R2 = 8; };
+template <> struct FePlan<9> { static constexpr int R0 = 16, R1 = 4, R2 = 8; };
+
+template <int LOGM>
+struct FeCfg {
+    using Plan = FePlan<LOGM>;
+    static constexpr int M = 1 << LOGM;
+    static constexpr int R0 = Plan::R0, R1 = Plan::R1, R2 = Plan::R2;
+    static_assert(R0 * R1 * R2 == M, "radix plan must cover M");
+    static constexpr int P = 2 * R2;                // points per thread
+    static constexpr int T = M / P;                 // threads per CTA
+    static constexpr int J = M / R2;                // butterflies of the last pass
+    static constexpr int PADSHIFT = (R0 == 32) ? 5 : 4;
+    static constexpr int N_PASS_HI = M / 64;
+    static constexpr int N_POST_HI = M / 64;
+    // shared memory layout (bytes)
+    static constexpr int OFF_X0 = 0;                   // int8 frame, buffer 0
+    static constexpr int OFF_X1 = 2 * M;               // int8 frame, buffer 1
+    static constexpr int OFF_D = 4 * M;                // padded complex data
+    static constexpr int OFF_PLO = OFF_D + (M + (M >> PADSHIFT)) * 8;
+    static constexpr int OFF_PHI = OFF_PLO + 64 * 8;
+    static constexpr int OFF_QLO = OFF_PHI + N_PASS_HI * 8;
+    static constexpr int OFF_QHI = OFF_QLO + 64 * 8;
+    static constexpr int OFF_BAR = (OFF_QHI + N_POST_HI * 8 + 15) / 16 * 16;
+    static constexpr int OFF_FLAG = OFF_BAR + 16;
+    static constexpr int SMEM = OFF_FLAG + 16;
+    // CTAs per SM the launch bounds plan for: as many as shared memory allows,
+    // with at most 128 registers per thread.
+    static constexpr int BY_SMEM = (220 * 1024) / SMEM;
+    static constexpr int BY_REGS = 65536 / (T * 128);
+    static constexpr int MIN_BLOCKS =
+        (BY_SMEM < BY_REGS ? BY_SMEM : BY_REGS) < 1 ? 1 : (BY_SMEM < BY_REGS ? BY_SMEM : BY_REGS);
+};
+
+// Shared-memory index padding: one float2 per R0 elements, which makes the
+// stride-R0 scatter of the first pass conflict-free and keeps every other
+// access a contiguous run.
+template <int SHIFT>
+__device__ __forceinline__ int padi(int i) { return i + (i >> SHIFT); }
+
+// Stockham pass of radix R over M points with sub-transform size NS:
 //   out[(j/NS)*NS*R + j%NS + r*NS] = DFT_R( in[j + r*M/R] * w^(r*(j%NS)) )
-// Each of the T threads owns P = M/T points, i.e. P/R butterflies. The pass
-// is in place: every thread reads all of its inputs, the CTA synchronises,
-// then every thread writes. The first pass reads int8 pairs instead.
-template <int M, int T, int R, int NS, bool FIRST>
+// Each thread owns P/R butterflies. In place: read all, barrier, write all,
+// barrier. The first pass reads int8 sample pairs instead of shared data.
+template <int M, int T, int P, int R, int NS, int SHIFT, bool FIRST>
 __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *__restrict__ sx,
                                          const float2 *lo, const float2 *hi, int tid) {
-    constexpr int P = M / T;
     constexpr int NB = P / R;
     constexpr int STRIDE = M / R;
     static_assert(NB >= 1 && NB * R == P, "bad radix plan");
@@ -186,13 +224,10 @@ __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *_
                 const char2 c = sx[i];
                 v[q][r] = make_float2(static_cast<float>(c.x), static_cast<float>(c.y));
             } else {
-                v[q][r] = sd[padi(i)];
+                v[q][r] = sd[padi<SHIFT>(i)];
             }
         }
-        if constexpr (NS > 1) {
-            const int u = (j & (NS - 1)) * (M / (NS * R));
-            apply_twiddles<R>(v[q], u, lo, hi);
-        }
+        if constexpr (NS > 1) apply_twiddles<R>(v[q], (j & (NS - 1)) * (M / (NS * R)), lo, hi);
         Dft<R>::run(v[q]);
     }
     __syncthreads();
@@ -201,45 +236,74 @@ __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *_
         const int j = tid + q * T;
         const int base = (j & ~(NS - 1)) * R + (j & (NS - 1));
 #pragma unroll
-        for (int r = 0; r < R; ++r) sd[padi(base + r * NS)] = v[q][r];
+        for (int r = 0; r < R; ++r) sd[padi<SHIFT>(base + r * NS)] = v[q][r];
     }
     __syncthreads();
 }
 
-template <int M, int T, int NS>
-__device__ __forceinline__ void fft_rest(float2 *sd, const float2 *lo, const float2 *hi,
-                                         int tid) {
-    if constexpr (NS < M) {
-        constexpr int REM = M / NS;
-        constexpr int R = REM >= 16 ? 16 : REM;
-        fft_pass<M, T, R, NS, false>(sd, nullptr, lo, hi, tid);
-        fft_rest<M, T, NS * R>(sd, lo, hi, tid);
+// X[k] = Fe + w_k Fo and X[M-k] = conj(Fe - w_k Fo), with Z = FFT of the packed
+// pairs, Fe = (Z[k] + conj(Z[M-k]))/2, Fo = -i (Z[k] - conj(Z[M-k]))/2 and
+// w_k = exp(-2*pi*i*k/L).
+// Where bin k of the current (frame, station) goes in the channel-tiled layout.
+struct YRow {
+    float2 *base;        // y + (f*n_station + s)*kYTile
+    size_t tile_stride;  // y_frames*n_station*kYTile
+    __device__ __forceinline__ float2 &operator[](int k) const {
+        return base[static_cast<size_t>(k / kYTile) * tile_stride + (k % kYTile)];
+    }
+};
+
+__device__ __forceinline__ void split_store(float2 zk, float2 zmk, int k, int M,
+                                            const float2 *qlo, const float2 *qhi,
+                                            const YRow &yrow) {
+    const float2 zm = make_float2(zmk.x, -zmk.y);
+    const float2 fe = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y + zm.y));
+    const float2 fo = make_float2(0.5f * (zk.y - zm.y), -0.5f * (zk.x - zm.x));
+    const float2 wf = cmul(cmul(qlo[k & 63], qhi[k >> 6]), fo);
+    yrow[k] = cadd(fe, wf);
+    yrow[M - k] = make_float2(fe.x - wf.x, wf.y - fe.y);
+}
+
+// Last pass (radix R2, NS = J) fused with the split and the global store.
+template <int LOGM>
+__device__ __forceinline__ void last_pass_store(const float2 *__restrict__ sd,
+                                                const float2 *plo, const float2 *phi,
+                                                const float2 *qlo, const float2 *qhi,
+                                                const YRow &yrow, int tid) {
+    using C = FeCfg<LOGM>;
+    constexpr int M = C::M, J = C::J, R = C::R2;
+    const int j1 = tid;
+    const int j2 = (tid == 0) ? J / 2 : J - tid;
+    float2 a[R], b[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        a[r] = sd[padi<C::PADSHIFT>(j1 + r * J)];
+        b[r] = sd[padi<C::PADSHIFT>(j2 + r * J)];
+    }
+    apply_twiddles<R>(a, j1, plo, phi);
+    apply_twiddles<R>(b, j2, plo, phi);
+    Dft<R>::run(a);   // a[r] = Z[j1 + r*J]
+    Dft<R>::run(b);   // b[r] = Z[j2 + r*J]
+    if (tid != 0) {
+        // Z[M - (j1 + r*J)] = Z[j2 + (R-1-r)*J]
+#pragma unroll
+        for (int r = 0; r < R; ++r) split_store(a[r], b[R - 1 - r], j1 + r * J, M, qlo, qhi, yrow);
+    } else {
+        // butterfly 0: k = r*J pairs with (R-r)*J; k = 0 gives the real DC bin,
+        // k = M/2 is its own partner: X[M/2] = conj(Z[M/2]).
+        yrow[0] = make_float2(a[0].x + a[0].y, 0.0f);
+#pragma unroll
+        for (int r = 1; r < R / 2; ++r) split_store(a[r], a[R - r], r * J, M, qlo, qhi, yrow);
+        yrow[M / 2] = make_float2(a[R / 2].x, -a[R / 2].y);
+        // butterfly J/2: k = J/2 + r*J pairs with J/2 + (R-1-r)*J.
+#pragma unroll
+        for (int r = 0; r < R / 2; ++r)
+            split_store(b[r], b[R - 1 - r], J / 2 + r * J, M, qlo, qhi, yrow);
     }
 }
 
 struct TwPtrs {
     const float2 *pass_lo, *pass_hi, *post_lo, *post_hi;
-};
-
-template <int LOGM>
-struct FeCfg {
-    static constexpr int M = 1 << LOGM;
-    static constexpr int P = (LOGM >= 13) ? 32 : 16;   // points per thread
-    static constexpr int T = M / P;                    // threads per CTA
-    static constexpr int N_PASS_HI = M / 64;
-    static constexpr int N_POST_HI = M / 128 + 1;
-    // shared memory layout (bytes)
-    static constexpr int OFF_X0 = 0;                   // int8 frame, buffer 0
-    static constexpr int OFF_X1 = 2 * M;               // int8 frame, buffer 1
-    static constexpr int OFF_D = 4 * M;                // padded complex data
-    static constexpr int OFF_PLO = OFF_D + (M + M / 16) * 8;
-    static constexpr int OFF_PHI = OFF_PLO + 64 * 8;
-    static constexpr int OFF_QLO = OFF_PHI + N_PASS_HI * 8;
-    static constexpr int OFF_QHI = OFF_QLO + 64 * 8;
-    static constexpr int OFF_BAR = (OFF_QHI + N_POST_HI * 8 + 15) / 16 * 16;
-    static constexpr int OFF_FLAG = OFF_BAR + 16;
-    static constexpr int SMEM = OFF_FLAG + 16;
-    static constexpr int MIN_BLOCKS = (LOGM >= 14) ? 1 : (LOGM == 13 ? 2 : 1);
 };
 
 __device__ __forceinline__ bool frame_present(const FengineArgs &a, int f, int s) {
@@ -306,14 +370,15 @@ __global__ void __launch_bounds__(FeCfg<LOGM>::T, FeCfg<LOGM>::MIN_BLOCKS)
         const int next = item + gridDim.x;
         bool next_issued = false;
         if (tid == 0 && next < n_items && present(next)) {
-            // The other buffer was last read by the previous item's first
-            // pass, which every thread finished before its first barrier.
+            // The other buffer was last read by the previous item's first pass,
+            // which every thread finished before that pass's first barrier.
             fence_proxy_async_smem();
             mbar_arrive_expect_tx(&bar[buf ^ 1], frame_bytes);
             bulk_copy_g2s(buf ? sx0 : sx1, src_of(next), frame_bytes, &bar[buf ^ 1]);
             next_issued = true;
         }
-        float2 *yrow = a.y + static_cast<size_t>(item) * M;
+        const YRow yrow{a.y + static_cast<size_t>(item) * kYTile,
+                        static_cast<size_t>(a.y_frames) * a.n_station * kYTile};
 
         if (!present(item)) {
             // Missing frame: its samples count as zeros, so does its spectrum.
@@ -333,27 +398,9 @@ __global__ void __launch_bounds__(FeCfg<LOGM>::T, FeCfg<LOGM>::MIN_BLOCKS)
         }
         parity_bits ^= 1u << buf;
 
-        fft_pass<M, T, 16, 1, true>(sd, buf ? sx1 : sx0, plo, phi, tid);
-        fft_rest<M, T, 16>(sd, plo, phi, tid);
-
-        // Real split: X[k] = Fe + w^k Fo, X[M-k] = conj(Fe - w^k Fo), with
-        // Fe = (Z[k] + conj(Z[M-k]))/2, Fo = -i (Z[k] - conj(Z[M-k]))/2.
-#pragma unroll 4
-        for (int k = tid; k < M / 2; k += T) {
-            const float2 zk = sd[padi(k)];
-            float2 zm = sd[padi((M - k) & (M - 1))];
-            zm.y = -zm.y;
-            const float2 fe = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y + zm.y));
-            const float2 fo = make_float2(0.5f * (zk.y - zm.y), -0.5f * (zk.x - zm.x));
-            const float2 w = cmul(qlo[k & 63], qhi[k >> 6]);
-            const float2 wf = cmul(w, fo);
-            yrow[k] = cadd(fe, wf);
-            if (k != 0) yrow[M - k] = make_float2(fe.x - wf.x, wf.y - fe.y);
-        }
-        if (tid == 0) {
-            const float2 zh = sd[padi(M / 2)];
-            yrow[M / 2] = make_float2(zh.x, -zh.y);
-        }
+        fft_pass<M, T, C::P, C::R0, 1, C::PADSHIFT, true>(sd, buf ? sx1 : sx0, plo, phi, tid);
+        fft_pass<M, T, C::P, C::R1, C::R0, C::PADSHIFT, false>(sd, nullptr, plo, phi, tid);
+        last_pass_store<LOGM>(sd, plo, phi, qlo, qhi, yrow, tid);
         // The next item's first pass synchronises before it overwrites sd.
     }
 }
@@ -401,7 +448,7 @@ corr_status fengine_prepare(int n_freq, TwiddleTables *tw) {
     const int M = n_freq;
     const double pi = 3.14159265358979323846;
     std::vector<float2> h_plo(64), h_phi(static_cast<size_t>(M / 64)), h_qlo(64),
-        h_qhi(static_cast<size_t>(M / 128 + 1));
+        h_qhi(static_cast<size_t>(M / 64));
     for (int u = 0; u < 64; ++u) {
         const double a = -2.0 * pi * u / M;
         h_plo[u] = make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
@@ -412,12 +459,12 @@ corr_status fengine_prepare(int n_freq, TwiddleTables *tw) {
         const double a = -2.0 * pi * 64.0 * u / M;
         h_phi[u] = make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
     }
-    for (int u = 0; u < M / 128 + 1; ++u) {
+    for (int u = 0; u < M / 64; ++u) {
         const double b = -pi * 64.0 * u / M;
         h_qhi[u] = make_float2(static_cast<float>(std::cos(b)), static_cast<float>(std::sin(b)));
     }
     tw->n_pass_hi = M / 64;
-    tw->n_post_hi = M / 128 + 1;
+    tw->n_post_hi = M / 64;
     const size_t n_all = 64 + h_phi.size() + 64 + h_qhi.size();
     float2 *d = nullptr;
     corr_status st = cuda_check(cudaMalloc(&d, n_all * sizeof(float2)), "cudaMalloc(twiddles)");

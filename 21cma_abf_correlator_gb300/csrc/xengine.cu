@@ -39,8 +39,8 @@ __device__ __forceinline__ void decode_pair(int p, int nb, int *bj, int *bk) {
 }
 
 __global__ void __launch_bounds__(1024, 1)
-    xengine_plain_kernel(const float2 *__restrict__ y, int n_station, int npad, int n_freq,
-                         int frames, float2 *__restrict__ acc, int pairs_per_cta,
+    xengine_plain_kernel(const float2 *__restrict__ y, int y_frames, int n_station, int npad,
+                         int n_freq, int frames, float2 *__restrict__ acc, int pairs_per_cta,
                          int n_pairs) {
     extern __shared__ __align__(16) float2 xs[];   // [stage][frame][npad][32]
     const int lane = threadIdx.x & 31;
@@ -67,8 +67,8 @@ __global__ void __launch_bounds__(1024, 1)
             const int st = row - fi * npad;
             const int f = f0 + fi;
             const bool ok = (st < n_station) && (f < frames);
-            const float2 *src =
-                ok ? y + (static_cast<size_t>(f) * n_station + st) * n_freq + c0 + part * 2 : y;
+            // two channels per 16-byte piece, inside one channel tile of the spectra
+            const float2 *src = ok ? y + y_index(c0 + part * 2, f, st, n_station, y_frames) : y;
             cp_async16(dst + row * kXch + part * 2, src, ok ? 16u : 0u);
         }
     };
@@ -188,7 +188,7 @@ corr_status xengine_plain_launch(const XengineArgs &a, int num_sms, cudaStream_t
     }
     dim3 grid(groups, a.n_freq / kXch);
     xengine_plain_kernel<<<grid, per_cta * 32, smem, stream>>>(
-        a.y, a.n_station, npad, a.n_freq, a.frames, a.acc, per_cta, n_pairs);
+        a.y, a.y_frames, a.n_station, npad, a.n_freq, a.frames, a.acc, per_cta, n_pairs);
     return cuda_check(cudaGetLastError(), "xengine_plain_kernel launch");
 }
 

@@ -195,6 +195,8 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--frames", type=int, default=0,
+                    help="override frames per integration (smaller cases for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -218,6 +220,9 @@ def main() -> None:
     synth = importlib.import_module(PKG_NAME + ".synth")
     abi = pkg.abi
     w = synth.WORKLOADS[args.workload]
+    if args.frames:
+        import dataclasses
+        w = dataclasses.replace(w, frames=args.frames)
     N, nf, F, L = w.n_station, w.n_freq, w.frames, w.fft_len
     B = w.n_baseline
 
