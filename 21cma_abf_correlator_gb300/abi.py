@@ -150,6 +150,9 @@ SIGNATURES = {
                                     C.c_size_t, C.c_int32, C.c_int32, C.c_void_p]),
     "corrx_run_xengine": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "corrx_selftest_watchdog": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
+    "corrx_accumulate_noalloc": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                                           C.c_size_t, C.c_size_t, C.c_void_p, C.c_size_t,
+                                           C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
 }
 
 _lib: C.CDLL | None = None

@@ -1,0 +1,167 @@
+// noalloc.cu -- corrx_accumulate for callers that cannot allocate device memory.
+//
+// Some hosts of this library may not call cudaMalloc at all: an application that
+// owns all device memory through its own pool and forbids allocation by plugins,
+// code running inside stream capture or a real-time loop where an allocation
+// (and the device-wide synchronisation it can imply) is not allowed, or a host
+// that links the library into a process whose memory budget is fixed up front.
+// corrx_accumulate_noalloc serves them: it runs the same F-engine and X-engine
+// kernels as corrx_accumulate, but the spectra between the two live in a
+// file-scope device array of fixed size instead of a buffer allocated by
+// corrx_create, and the twiddle tables are computed into a second fixed array.
+//
+// Properties a caller must know:
+//   * scratch: kNoAllocScratchBytes (64 MiB) of spectra plus a few KB of twiddle
+//     tables, held by every GPU that loads the library until the process exits;
+//   * one call may cover at most 64 MiB / (n_station * n_freq * 8) frames (21 at
+//     24 inputs and n_freq 16384); larger requests are rejected with
+//     CORR_ERR_ARG, nothing is launched, and the caller splits them;
+//   * the first call on a device looks up the arrays' device addresses
+//     (cudaGetSymbolAddress) with that device current; make that first call
+//     before any stream capture;
+//   * every call shares the arrays: two calls whose kernels overlap on the GPU
+//     (different streams, no ordering between them) race on the scratch and
+//     give wrong results. Calls on one stream are ordered and safe. Nothing has
+//     to start at zero: each call writes every scratch value it reads;
+//   * a bounded wait that runs out inside a kernel ends that kernel early
+//     without a report (there is no engine to hold a watchdog flag); use
+//     corrx_accumulate where that report matters.
+
+#include <cmath>
+#include <mutex>
+
+#include "engine.h"
+
+namespace corrgb {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;
+constexpr int kMaxFreq = 16384;
+constexpr int kTwEntries = 64 + kMaxFreq / 64 + 64 + kMaxFreq / 64;
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) float2 g_noalloc_spectra[kNoAllocScratchBytes / sizeof(float2)];
+static __device__ __align__(256) float2 g_noalloc_twiddles[kTwEntries];
+
+struct DeviceScratch {
+    float2 *spectra = nullptr;
+    float2 *twiddles = nullptr;
+    int num_sms = 0;
+    bool ready = false;
+};
+
+std::mutex g_mu;
+DeviceScratch g_dev[kMaxDevices];
+
+// Device addresses of the scratch arrays on `dev` (current), looked up once.
+corr_status scratch_for(int dev, DeviceScratch *out) {
+    if (dev < 0 || dev >= kMaxDevices) return failf(CORR_ERR_ARG, "device %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_mu);
+    DeviceScratch &d = g_dev[dev];
+    if (!d.ready) {
+        void *p = nullptr;
+        corr_status st = cuda_check(cudaGetSymbolAddress(&p, g_noalloc_spectra),
+                                    "cudaGetSymbolAddress(spectra scratch)");
+        if (st != CORR_OK) return st;
+        d.spectra = static_cast<float2 *>(p);
+        st = cuda_check(cudaGetSymbolAddress(&p, g_noalloc_twiddles),
+                        "cudaGetSymbolAddress(twiddle scratch)");
+        if (st != CORR_OK) return st;
+        d.twiddles = static_cast<float2 *>(p);
+        st = cuda_check(cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, dev),
+                        "cudaDeviceGetAttribute(SM count)");
+        if (st != CORR_OK) return st;
+        d.ready = true;
+    }
+    *out = d;
+    return CORR_OK;
+}
+
+// The F-engine's four twiddle tables (layout of TwiddleTables, engine.h) for
+// transform length M, in double precision rounded once to float.
+__global__ void noalloc_twiddle_kernel(float2 *tw, int M) {
+    const int n_hi = M / 64;
+    const int total = 64 + n_hi + 64 + n_hi;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        double x;   // angle / pi
+        if (i < 64) x = -2.0 * i / M;                                   // pass_lo
+        else if (i < 64 + n_hi) x = -2.0 * 64.0 * (i - 64) / M;          // pass_hi
+        else if (i < 128 + n_hi) x = -1.0 * (i - 64 - n_hi) / M;          // post_lo
+        else x = -64.0 * (i - 128 - n_hi) / M;                           // post_hi
+        double s, c;
+        sincospi(x, &s, &c);
+        tw[i] = make_float2(static_cast<float>(c), static_cast<float>(s));
+    }
+}
+
+} // namespace
+} // namespace corrgb
+
+using namespace corrgb;
+
+extern "C" corr_status corrx_accumulate_noalloc(int32_t n_station, int32_t n_freq, int32_t xmode,
+                                                const int8_t *d_samples, size_t station_stride,
+                                                size_t frame_stride, const uint8_t *d_mask,
+                                                size_t mask_station_stride, int32_t mask_bit0,
+                                                int32_t frames, void *d_acc, void *stream) {
+    corr_status st = check_geometry(n_station, n_freq);
+    if (st != CORR_OK) return st;
+    if (xmode != CORR_X_PLAIN_FP32 && xmode != CORR_X_TC_FP16 && xmode != CORR_X_TC_FP16_SPLIT)
+        return failf(CORR_ERR_ARG, "unknown X-engine mode %d", xmode);
+    if (d_samples == nullptr || d_acc == nullptr)
+        return fail(CORR_ERR_ARG, "d_samples and d_acc must not be NULL");
+    if (frames < 0 || mask_bit0 < 0) return fail(CORR_ERR_ARG, "frames and mask_bit0 must be >= 0");
+    if (frame_stride < 2u * static_cast<size_t>(n_freq))
+        return fail(CORR_ERR_ARG, "frame_stride is shorter than a frame");
+    if ((reinterpret_cast<uintptr_t>(d_samples) | station_stride | frame_stride) % 16 != 0)
+        return fail(CORR_ERR_ARG, "samples, station_stride and frame_stride must be 16-byte aligned");
+    const size_t per_frame = static_cast<size_t>(n_station) * n_freq * sizeof(float2);
+    const int max_frames = static_cast<int>(kNoAllocScratchBytes / per_frame);
+    if (frames > max_frames)
+        return failf(CORR_ERR_ARG,
+                     "frames=%d exceeds the %d frames the fixed %zu-byte scratch holds at "
+                     "n_station=%d, n_freq=%d; split the call",
+                     frames, max_frames, kNoAllocScratchBytes, n_station, n_freq);
+    if (frames == 0) return CORR_OK;
+
+    int dev = 0;
+    if ((st = cuda_check(cudaGetDevice(&dev), "cudaGetDevice")) != CORR_OK) return st;
+    DeviceScratch d;
+    if ((st = scratch_for(dev, &d)) != CORR_OK) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+    noalloc_twiddle_kernel<<<4, 256, 0, s>>>(d.twiddles, n_freq);
+    if ((st = cuda_check(cudaGetLastError(), "noalloc_twiddle_kernel launch")) != CORR_OK) return st;
+    TwiddleTables tw;
+    tw.n_pass_hi = n_freq / 64;
+    tw.n_post_hi = n_freq / 64;
+    tw.pass_lo = d.twiddles;
+    tw.pass_hi = tw.pass_lo + 64;
+    tw.post_lo = tw.pass_hi + tw.n_pass_hi;
+    tw.post_hi = tw.post_lo + 64;
+
+    FengineArgs fa{};
+    fa.samples = d_samples;
+    fa.station_stride = station_stride;
+    fa.frame_stride = frame_stride;
+    fa.mask = d_mask;
+    fa.mask_station_stride = mask_station_stride;
+    fa.mask_bit0 = mask_bit0;
+    fa.n_station = n_station;
+    fa.frames = frames;
+    fa.y = d.spectra;
+    fa.y_frames = frames;
+    fa.err = nullptr;
+    if ((st = fengine_launch(n_freq, tw, fa, d.num_sms, s)) != CORR_OK) return st;
+
+    XengineArgs xa{};
+    xa.y = d.spectra;
+    xa.y_frames = frames;
+    xa.n_station = n_station;
+    xa.n_freq = n_freq;
+    xa.frames = frames;
+    xa.acc = static_cast<float2 *>(d_acc);
+    xa.err = nullptr;
+    if (xmode == CORR_X_PLAIN_FP32) return xengine_plain_launch(xa, d.num_sms, s);
+    return xengine_tc_launch(xa, xmode == CORR_X_TC_FP16_SPLIT, d.num_sms, s);
+}

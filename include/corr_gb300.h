@@ -87,6 +87,27 @@ corr_status corrx_run_xengine(void *eng, int32_t frames, void *d_acc, void *stre
    the timeout path of every bounded wait can be exercised without hanging a GPU. */
 corr_status corrx_selftest_watchdog(void *eng, int64_t budget_cycles, void *stream);
 
+/*
+ * corrx_accumulate without any device allocation. No counterpart in the
+ * reference. For callers that may not call cudaMalloc (a host that owns all
+ * device memory through its own pool, code inside stream capture or a
+ * real-time loop, a process with a fixed memory budget): the spectra between
+ * the F- and X-engine live in a fixed 64 MiB device array inside the library
+ * (held by every GPU that loads it until exit), so one call covers at most
+ * 64 MiB / (n_station * n_freq * 8) frames -- 21 at 24 inputs and n_freq 16384;
+ * more is rejected with CORR_ERR_ARG. Same arguments and result as
+ * corrx_accumulate (d_acc += visibilities), plus the geometry and X-engine that
+ * an engine would otherwise carry. The first call on a device looks up the
+ * array's address with that device current: make it before any stream capture.
+ * All calls share the array: calls whose kernels overlap on the GPU race, calls
+ * ordered on one stream do not. Nothing in it needs to start at zero.
+ */
+corr_status corrx_accumulate_noalloc(int32_t n_station, int32_t n_freq, int32_t xmode,
+                                     const int8_t *d_samples, size_t station_stride,
+                                     size_t frame_stride, const uint8_t *d_mask,
+                                     size_t mask_station_stride, int32_t mask_bit0,
+                                     int32_t frames, void *d_acc, void *stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif
