@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "engine.h"
 
@@ -72,6 +73,10 @@ corr_status fxplan_create(int device, int n_station, int n_freq, int max_frames,
     corr_status st = check_geometry(n_station, n_freq);
     if (st != CORR_OK) return st;
     if (max_frames < 1) return fail(CORR_ERR_ARG, "max_frames must be >= 1");
+    if (static_cast<uint64_t>(max_frames) * n_station * n_freq >= (uint64_t(1) << 32))
+        return failf(CORR_ERR_ARG,
+                     "max_frames=%d: the spectra buffer would hold 2^32 or more values",
+                     max_frames);
     if (xmode != CORR_X_PLAIN_FP32 && xmode != CORR_X_TC_FP16 && xmode != CORR_X_TC_FP16_SPLIT)
         return failf(CORR_ERR_ARG, "unknown X-engine mode %d", xmode);
     if ((st = cuda_check(cudaSetDevice(device), "cudaSetDevice")) != CORR_OK) return st;
@@ -83,6 +88,7 @@ corr_status fxplan_create(int device, int n_station, int n_freq, int max_frames,
     p->n_freq = n_freq;
     p->n_baseline = n_station * (n_station + 1) / 2;
     p->max_frames = max_frames;
+    p->ytile = ytile_for(n_station);
     p->xmode = xmode;
     if ((st = cuda_check(cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount,
                                                 device),
@@ -142,12 +148,14 @@ corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_s
         fa.frames = ft;
         fa.y = p->d_y;
         fa.y_frames = p->max_frames;
+        fa.ytile = p->ytile;
         fa.err = p->d_err;
         corr_status st = fengine_launch(p->n_freq, p->tw, fa, p->num_sms, stream);
         if (st != CORR_OK) return st;
         XengineArgs xa{};
         xa.y = p->d_y;
         xa.y_frames = p->max_frames;
+        xa.ytile = p->ytile;
         xa.n_station = p->n_station;
         xa.n_freq = p->n_freq;
         xa.frames = ft;
@@ -262,6 +270,7 @@ extern "C" corr_status corrx_run_fengine(void *eng, const int8_t *d_samples,
     fa.frames = frames;
     fa.y = p->d_y;
     fa.y_frames = p->max_frames;
+    fa.ytile = p->ytile;
     fa.err = p->d_err;
     return fengine_launch(p->n_freq, p->tw, fa, p->num_sms, static_cast<cudaStream_t>(stream));
 }
@@ -277,6 +286,7 @@ extern "C" corr_status corrx_run_xengine(void *eng, int32_t frames, void *d_acc,
     XengineArgs xa{};
     xa.y = p->d_y;
     xa.y_frames = p->max_frames;
+    xa.ytile = p->ytile;
     xa.n_station = p->n_station;
     xa.n_freq = p->n_freq;
     xa.frames = frames;
@@ -302,4 +312,177 @@ extern "C" corr_status corrx_check(void *eng) {
     FxPlan *p = static_cast<FxPlan *>(eng);
     if (p == nullptr) return fail(CORR_ERR_ARG, "eng is NULL");
     return fxplan_check(p);
+}
+
+// ---------------------------------------------------------------------------
+// Batched integration blocks captured in one CUDA graph.
+// ---------------------------------------------------------------------------
+
+namespace corrgb {
+namespace {
+
+struct FxBatch {
+    FxPlan *plan = nullptr;
+    int n_blocks = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<cudaEvent_t> ev_fork;
+    unsigned long long *d_stamps = nullptr;   // [block][start, row in host memory], ns
+    cudaStream_t cap = nullptr, side = nullptr;
+    cudaStream_t last_launch = nullptr;
+};
+
+void batch_free(FxBatch *b) {
+    if (b == nullptr) return;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (cudaEvent_t e : b->ev_fork)
+        if (e) cudaEventDestroy(e);
+    if (b->d_stamps) cudaFree(b->d_stamps);
+    if (b->cap) cudaStreamDestroy(b->cap);
+    if (b->side) cudaStreamDestroy(b->side);
+    delete b;
+}
+
+} // namespace
+} // namespace corrgb
+
+extern "C" corr_status corrx_batch_create(void *eng, const int8_t *d_samples,
+                                          size_t station_stride, size_t frame_stride,
+                                          const uint8_t *d_mask, size_t mask_station_stride,
+                                          const int64_t *block_first, const int32_t *block_frames,
+                                          int32_t n_blocks, void *d_rows, void *h_rows,
+                                          void **out_batch) {
+    using namespace corrgb;
+    if (out_batch == nullptr) return fail(CORR_ERR_ARG, "out_batch is NULL");
+    *out_batch = nullptr;
+    FxPlan *p = static_cast<FxPlan *>(eng);
+    if (p == nullptr || d_samples == nullptr || d_rows == nullptr || block_first == nullptr ||
+        block_frames == nullptr)
+        return fail(CORR_ERR_ARG, "eng, d_samples, d_rows and the block arrays must be non-NULL");
+    if (n_blocks < 1) return fail(CORR_ERR_ARG, "n_blocks must be >= 1");
+    for (int i = 0; i < n_blocks; ++i)
+        if (block_frames[i] < 1 || block_first[i] < 0)
+            return failf(CORR_ERR_ARG, "block %d: first=%lld frames=%d", i,
+                         (long long)block_first[i], block_frames[i]);
+    corr_status st = cuda_check(cudaSetDevice(p->device), "cudaSetDevice");
+    if (st != CORR_OK) return st;
+    FxBatch *b = new (std::nothrow) FxBatch();
+    if (b == nullptr) return fail(CORR_ERR_NOMEM, "cannot allocate the batch");
+    b->plan = p;
+    b->n_blocks = n_blocks;
+    const size_t row_elems = static_cast<size_t>(p->n_baseline) * p->n_freq;
+    float2 *rows = static_cast<float2 *>(d_rows);
+    if ((st = cuda_check(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking),
+                         "cudaStreamCreate(capture)")) != CORR_OK ||
+        (st = cuda_check(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking),
+                         "cudaStreamCreate(side)")) != CORR_OK) {
+        batch_free(b);
+        return st;
+    }
+    b->ev_fork.assign(n_blocks + 1, nullptr);
+    st = cuda_check(cudaMalloc(&b->d_stamps, 2 * sizeof(unsigned long long) * n_blocks),
+                    "cudaMalloc(stamps)");
+    if (st == CORR_OK)
+        st = cuda_check(cudaMemset(b->d_stamps, 0, 2 * sizeof(unsigned long long) * n_blocks),
+                        "cudaMemset(stamps)");
+    for (int i = 0; i <= n_blocks && st == CORR_OK; ++i)
+        st = cuda_check(cudaEventCreateWithFlags(&b->ev_fork[i], cudaEventDisableTiming),
+                        "cudaEventCreate");
+    if (st != CORR_OK) {
+        batch_free(b);
+        return st;
+    }
+    // Kernels configure themselves on first use; do that outside the capture.
+    st = fxplan_accumulate(p, d_samples, station_stride, frame_stride, d_mask,
+                           mask_station_stride, static_cast<int>(block_first[0]), 1, rows,
+                           b->cap);
+    if (st == CORR_OK) st = cuda_check(cudaStreamSynchronize(b->cap), "warm-up");
+    if (st != CORR_OK) {
+        batch_free(b);
+        return st;
+    }
+
+    st = cuda_check(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal),
+                    "cudaStreamBeginCapture");
+    for (int i = 0; i < n_blocks && st == CORR_OK; ++i) {
+        float2 *row = rows + static_cast<size_t>(i) * row_elems;
+        const int first = static_cast<int>(block_first[i]);
+        if ((st = stamp_launch(b->d_stamps + 2 * i, b->cap)) != CORR_OK) break;
+        if ((st = cuda_check(cudaMemsetAsync(row, 0, row_elems * sizeof(float2), b->cap),
+                             "cudaMemsetAsync(row)")) != CORR_OK)
+            break;
+        if ((st = fxplan_accumulate(p, d_samples + static_cast<size_t>(first) * frame_stride,
+                                    station_stride, frame_stride, d_mask, mask_station_stride,
+                                    first, block_frames[i], row, b->cap)) != CORR_OK)
+            break;
+        if ((st = scale_launch(row, row_elems, 1.0f / static_cast<float>(block_frames[i]),
+                               b->cap)) != CORR_OK)
+            break;
+        // dump on the side stream; the next block's kernels do not wait for it
+        if ((st = cuda_check(cudaEventRecord(b->ev_fork[i], b->cap), "cudaEventRecord")) != CORR_OK ||
+            (st = cuda_check(cudaStreamWaitEvent(b->side, b->ev_fork[i], 0), "cudaStreamWaitEvent")) !=
+                CORR_OK)
+            break;
+        if (h_rows != nullptr &&
+            (st = cuda_check(cudaMemcpyAsync(static_cast<float2 *>(h_rows) + i * row_elems, row,
+                                             row_elems * sizeof(float2), cudaMemcpyDeviceToHost,
+                                             b->side),
+                             "cudaMemcpyAsync(row dump)")) != CORR_OK)
+            break;
+        if ((st = stamp_launch(b->d_stamps + 2 * i + 1, b->side)) != CORR_OK) break;
+    }
+    // join the side stream back into the capture
+    if (st == CORR_OK)
+        st = cuda_check(cudaEventRecord(b->ev_fork[n_blocks], b->side), "cudaEventRecord");
+    if (st == CORR_OK)
+        st = cuda_check(cudaStreamWaitEvent(b->cap, b->ev_fork[n_blocks], 0), "cudaStreamWaitEvent");
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(b->cap, &g);
+    if (st == CORR_OK) st = cuda_check(e, "cudaStreamEndCapture");
+    b->graph = g;
+    if (st == CORR_OK)
+        st = cuda_check(cudaGraphInstantiate(&b->exec, b->graph, 0), "cudaGraphInstantiate");
+    if (st != CORR_OK) {
+        batch_free(b);
+        return st;
+    }
+    *out_batch = b;
+    return CORR_OK;
+}
+
+extern "C" corr_status corrx_batch_launch(void *batch, void *stream) {
+    using namespace corrgb;
+    FxBatch *b = static_cast<FxBatch *>(batch);
+    if (b == nullptr) return fail(CORR_ERR_ARG, "batch is NULL");
+    corr_status st = cuda_check(cudaSetDevice(b->plan->device), "cudaSetDevice");
+    if (st != CORR_OK) return st;
+    b->last_launch = static_cast<cudaStream_t>(stream);
+    return cuda_check(cudaGraphLaunch(b->exec, b->last_launch), "cudaGraphLaunch");
+}
+
+extern "C" corr_status corrx_batch_block_ms(void *batch, float *out_ms, int32_t n) {
+    using namespace corrgb;
+    FxBatch *b = static_cast<FxBatch *>(batch);
+    if (b == nullptr || out_ms == nullptr) return fail(CORR_ERR_ARG, "batch and out_ms must be non-NULL");
+    if (n < b->n_blocks) return failf(CORR_ERR_ARG, "n=%d < %d blocks", n, b->n_blocks);
+    corr_status st = cuda_check(cudaSetDevice(b->plan->device), "cudaSetDevice");
+    if (st == CORR_OK) st = cuda_check(cudaStreamSynchronize(b->last_launch), "cudaStreamSynchronize");
+    std::vector<unsigned long long> t(2 * static_cast<size_t>(b->n_blocks));
+    if (st == CORR_OK)
+        st = cuda_check(cudaMemcpy(t.data(), b->d_stamps, t.size() * sizeof(t[0]),
+                                   cudaMemcpyDeviceToHost),
+                        "cudaMemcpy(stamps)");
+    if (st != CORR_OK) return st;
+    for (int i = 0; i < b->n_blocks; ++i) {
+        if (t[2 * i] == 0 || t[2 * i + 1] < t[2 * i])
+            return failf(CORR_ERR_STATE, "block %d has no latency record (launch the batch first)", i);
+        out_ms[i] = static_cast<float>(static_cast<double>(t[2 * i + 1] - t[2 * i]) * 1e-6);
+    }
+    return CORR_OK;
+}
+
+extern "C" corr_status corrx_batch_destroy(void *batch) {
+    corrgb::batch_free(static_cast<corrgb::FxBatch *>(batch));
+    return CORR_OK;
 }

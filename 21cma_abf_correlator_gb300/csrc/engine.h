@@ -11,6 +11,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <algorithm>
 #include <string>
 
 #include <cuda_runtime.h>
@@ -52,15 +53,24 @@ struct TwiddleTables {
     int n_post_hi = 0;
 };
 
-/// Spectra layout shared by the F- and X-engines: channel-tiled,
-///   y[((c / kYTile) * y_frames + f) * n_station + s) * kYTile + c % kYTile]
-/// so one channel tile of every station over consecutive frames is a single
-/// contiguous block (what an X-engine CTA streams with one bulk copy per stage).
-constexpr int kYTile = 4;
+/// Spectra layout shared by the F- and X-engines: channel tiles of `ytile`
+/// channels (a power of two), each tile holding every frame and station,
+///   y[((c / ytile) * y_frames + f) * n_station + s) * ytile + c % ytile]
+/// ytile is the tensor X-engine's channels per CTA, so the KT frames x N
+/// stations of one tile that a CTA consumes per stage are one contiguous block
+/// (one bulk copy), while a warp of the F-engine still writes whole 32-byte
+/// sectors (32 consecutive bins = 32/ytile pieces of ytile*8 bytes).
+__host__ __device__ inline size_t y_index(int c, int f, int s, int n_station, int y_frames,
+                                          int ytile) {
+    return ((static_cast<size_t>(c / ytile) * y_frames + f) * n_station + s) * ytile +
+           (c % ytile);
+}
 
-__host__ __device__ inline size_t y_index(int c, int f, int s, int n_station, int y_frames) {
-    return ((static_cast<size_t>(c / kYTile) * y_frames + f) * n_station + s) * kYTile +
-           (c % kYTile);
+/// Channels per spectra tile for n_station inputs: 8 while 8 accumulators of
+/// 2N (rounded to 16) TMEM columns fit in 512 columns (N <= 32), else 4.
+inline int ytile_for(int n_station) {
+    const int n_mma = std::max(16, (2 * n_station + 15) / 16 * 16);
+    return 8 * n_mma <= 512 ? 8 : 4;
 }
 
 /// Arguments of one F-engine launch: `frames` x `n_station` real FFTs.
@@ -73,8 +83,9 @@ struct FengineArgs {
     int mask_bit0;
     int n_station;
     int frames;
-    float2 *y;                  // spectra, channel-tiled (y_index)
+    float2 *y;                  // spectra (y_index)
     int y_frames;               // frames the spectra buffer holds
+    int ytile;                  // channels per spectra tile
     int *err;
 };
 
@@ -82,6 +93,7 @@ struct FengineArgs {
 struct XengineArgs {
     const float2 *y;            // as FengineArgs::y
     int y_frames;               // frames the spectra buffer holds (>= frames)
+    int ytile;                  // channels per spectra tile
     int n_station;
     int n_freq;
     int frames;
@@ -99,6 +111,7 @@ corr_status fengine_launch(int n_freq, const TwiddleTables &tw, const FengineArg
 corr_status xengine_plain_launch(const XengineArgs &a, int num_sms, cudaStream_t stream);
 corr_status scale_launch(float2 *acc, size_t n, float s, cudaStream_t stream);
 corr_status watchdog_selftest_launch(int *err, long long budget_cycles, cudaStream_t stream);
+corr_status stamp_launch(unsigned long long *slot, cudaStream_t stream);
 
 // xengine_tc.cu
 size_t xengine_tc_workspace_bytes(int n_station, int n_freq);
@@ -113,6 +126,7 @@ struct FxPlan {
     int n_freq = 0;
     int n_baseline = 0;
     int max_frames = 0;   // frames per F/X pass (spectra buffer depth)
+    int ytile = 8;        // channels per spectra tile (ytile_for(n_station))
     int xmode = CORR_X_PLAIN_FP32;
     int num_sms = 0;
     float2 *d_y = nullptr;

@@ -18,10 +18,10 @@
 //     bins 0..M-1 are written, the Nyquist bin M is dropped and nothing is
 //     normalised (reference semantics, HANDOFF.md:583-602).
 //
-// Output layout: complex64, channel-tiled (engine.h, y_index): bin k of
-// (frame f, station s) lands in tile k/4 at ((k/4)*y_frames + f)*n_station + s,
-// slot k%4. A warp's 32 consecutive bins are eight whole 32-byte sectors, and
-// an X-engine CTA then reads its tiles over many frames as contiguous blocks.
+// Output layout (engine.h, y_index): complex64 in channel tiles of `ytile`
+// bins; bin k of (frame f, station s) lands at
+// ((k/ytile)*y_frames + f)*n_station + s)*ytile + k%ytile. The fused last pass
+// writes 32 consecutive bins per warp store: whole pieces of ytile*8 bytes.
 
 #include <cmath>
 #include <vector>
@@ -213,19 +213,27 @@ __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *_
     constexpr int NB = P / R;
     constexpr int STRIDE = M / R;
     static_assert(NB >= 1 && NB * R == P, "bad radix plan");
+    // Every index below is a padded per-thread base plus a compile-time offset:
+    // the read stride and the write stride are multiples of the padding period
+    // (or, for the first pass, offsets stay inside one period).
+    static_assert(STRIDE % (1 << SHIFT) == 0, "read stride");
+    static_assert(NS % (1 << SHIFT) == 0 || (NS == 1 && R == (1 << SHIFT)), "write stride");
+    constexpr int PSTRIDE = STRIDE + (STRIDE >> SHIFT);
+    constexpr int PNS = (NS == 1) ? 1 : NS + (NS >> SHIFT);
     float2 v[NB][R];
 #pragma unroll
     for (int q = 0; q < NB; ++q) {
         const int j = tid + q * T;
+        if constexpr (FIRST) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const int i = j + r * STRIDE;
-            if constexpr (FIRST) {
-                const char2 c = sx[i];
+            for (int r = 0; r < R; ++r) {
+                const char2 c = sx[j + r * STRIDE];
                 v[q][r] = make_float2(static_cast<float>(c.x), static_cast<float>(c.y));
-            } else {
-                v[q][r] = sd[padi<SHIFT>(i)];
             }
+        } else {
+            const int pj = padi<SHIFT>(j);
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[q][r] = sd[pj + r * PSTRIDE];
         }
         if constexpr (NS > 1) apply_twiddles<R>(v[q], (j & (NS - 1)) * (M / (NS * R)), lo, hi);
         Dft<R>::run(v[q]);
@@ -234,72 +242,91 @@ __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *_
 #pragma unroll
     for (int q = 0; q < NB; ++q) {
         const int j = tid + q * T;
-        const int base = (j & ~(NS - 1)) * R + (j & (NS - 1));
+        const int pb = padi<SHIFT>((j & ~(NS - 1)) * R + (j & (NS - 1)));
 #pragma unroll
-        for (int r = 0; r < R; ++r) sd[padi<SHIFT>(base + r * NS)] = v[q][r];
+        for (int r = 0; r < R; ++r) sd[pb + r * PNS] = v[q][r];
     }
     __syncthreads();
 }
 
-// X[k] = Fe + w_k Fo and X[M-k] = conj(Fe - w_k Fo), with Z = FFT of the packed
-// pairs, Fe = (Z[k] + conj(Z[M-k]))/2, Fo = -i (Z[k] - conj(Z[M-k]))/2 and
-// w_k = exp(-2*pi*i*k/L).
 // Where bin k of the current (frame, station) goes in the channel-tiled layout.
+// (Element indices fit 32 bits: the spectra buffer holds < 2^32 values.)
 struct YRow {
-    float2 *base;        // y + (f*n_station + s)*kYTile
-    size_t tile_stride;  // y_frames*n_station*kYTile
+    float2 *base;          // y + (f*n_station + s)*ytile
+    uint32_t tile_stride;  // y_frames*n_station*ytile
+    int shift;             // log2(ytile)
     __device__ __forceinline__ float2 &operator[](int k) const {
-        return base[static_cast<size_t>(k / kYTile) * tile_stride + (k % kYTile)];
+        return base[static_cast<uint32_t>(k >> shift) * tile_stride +
+                    static_cast<uint32_t>(k & ((1 << shift) - 1))];
     }
 };
 
-__device__ __forceinline__ void split_store(float2 zk, float2 zmk, int k, int M,
-                                            const float2 *qlo, const float2 *qhi,
-                                            const YRow &yrow) {
+// X[k] = Fe + w_k Fo and X[M-k] = conj(Fe - w_k Fo), with Z = FFT of the packed
+// pairs, Fe = (Z[k] + conj(Z[M-k]))/2, Fo = -i (Z[k] - conj(Z[M-k]))/2 and
+// w_k = exp(-2*pi*i*k/L) passed in. `both` = false skips X[M-k] (k = 0: Nyquist).
+__device__ __forceinline__ void split_store(float2 zk, float2 zmk, float2 w, int k, int M,
+                                            bool both, const YRow &yrow) {
     const float2 zm = make_float2(zmk.x, -zmk.y);
     const float2 fe = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y + zm.y));
     const float2 fo = make_float2(0.5f * (zk.y - zm.y), -0.5f * (zk.x - zm.x));
-    const float2 wf = cmul(cmul(qlo[k & 63], qhi[k >> 6]), fo);
+    const float2 wf = cmul(w, fo);
     yrow[k] = cadd(fe, wf);
-    yrow[M - k] = make_float2(fe.x - wf.x, wf.y - fe.y);
+    if (both) yrow[M - k] = make_float2(fe.x - wf.x, wf.y - fe.y);
 }
 
 // Last pass (radix R2, NS = J) fused with the split and the global store.
+// Thread t >= 1 owns butterflies t and J - t: Z[M - (t + r*J)] = Z[(J - t) + (R-1-r)*J],
+// so its R pairs are (a[r], b[R-1-r]). Thread 0 owns the two self-paired
+// butterflies 0 and J/2: pairs (a[r], a[R-r]) and (b[r], b[R-1-r]). All threads
+// run the same R iterations (thread 0's operands are register selects), so no
+// warp diverges; only X[M/2] = conj(Z[M/2]) is one extra store for thread 0.
+// Split twiddles: k = j + i*J gives w_k = w_j * exp(-pi*i*i/R2), one table
+// lookup per butterfly times compile-time constants.
 template <int LOGM>
 __device__ __forceinline__ void last_pass_store(const float2 *__restrict__ sd,
                                                 const float2 *plo, const float2 *phi,
                                                 const float2 *qlo, const float2 *qhi,
                                                 const YRow &yrow, int tid) {
     using C = FeCfg<LOGM>;
-    constexpr int M = C::M, J = C::J, R = C::R2;
+    constexpr int M = C::M, J = C::J, R = C::R2, H = R / 2;
+    static_assert(J % (1 << C::PADSHIFT) == 0, "last-pass stride");
+    constexpr int PJ = J + (J >> C::PADSHIFT);
+    const bool t0 = (tid == 0);
     const int j1 = tid;
-    const int j2 = (tid == 0) ? J / 2 : J - tid;
+    const int j2 = t0 ? J / 2 : J - tid;
     float2 a[R], b[R];
+    const int p1 = padi<C::PADSHIFT>(j1), p2 = padi<C::PADSHIFT>(j2);
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-        a[r] = sd[padi<C::PADSHIFT>(j1 + r * J)];
-        b[r] = sd[padi<C::PADSHIFT>(j2 + r * J)];
+        a[r] = sd[p1 + r * PJ];
+        b[r] = sd[p2 + r * PJ];
     }
     apply_twiddles<R>(a, j1, plo, phi);
     apply_twiddles<R>(b, j2, plo, phi);
     Dft<R>::run(a);   // a[r] = Z[j1 + r*J]
     Dft<R>::run(b);   // b[r] = Z[j2 + r*J]
-    if (tid != 0) {
-        // Z[M - (j1 + r*J)] = Z[j2 + (R-1-r)*J]
+    const float2 w1 = cmul(qlo[j1 & 63], qhi[j1 >> 6]);   // w_{j1}
+    const float2 w2 = cmul(qlo[j2 & 63], qhi[j2 >> 6]);   // w_{j2} (thread 0: w_{J/2})
 #pragma unroll
-        for (int r = 0; r < R; ++r) split_store(a[r], b[R - 1 - r], j1 + r * J, M, qlo, qhi, yrow);
-    } else {
-        // butterfly 0: k = r*J pairs with (R-r)*J; k = 0 gives the real DC bin,
-        // k = M/2 is its own partner: X[M/2] = conj(Z[M/2]).
-        yrow[0] = make_float2(a[0].x + a[0].y, 0.0f);
-#pragma unroll
-        for (int r = 1; r < R / 2; ++r) split_store(a[r], a[R - r], r * J, M, qlo, qhi, yrow);
-        yrow[M / 2] = make_float2(a[R / 2].x, -a[R / 2].y);
-        // butterfly J/2: k = J/2 + r*J pairs with J/2 + (R-1-r)*J.
-#pragma unroll
-        for (int r = 0; r < R / 2; ++r)
-            split_store(b[r], b[R - 1 - r], J / 2 + r * J, M, qlo, qhi, yrow);
+    for (int i = 0; i < R; ++i) {
+        float2 zk = a[i], zmk = b[R - 1 - i];
+        int k = j1 + i * J;
+        // exp(-pi*i*n/R) = exp(-2*pi*i*n*(16/R)/32)
+        float2 w = mul_w32(w1, i * (16 / R));
+        if (i < H) {
+            if (t0) {
+                zmk = a[(R - i) % R];
+                k = i * J;
+            }
+        } else if (t0) {
+            zk = b[i - H];
+            zmk = b[R - 1 - (i - H)];
+            k = J / 2 + (i - H) * J;
+            w = mul_w32(w2, (i - H) * (16 / R));
+        }
+        split_store(zk, zmk, w, k, M, !(t0 && i == 0), yrow);
     }
+    if (t0) yrow[M / 2] = make_float2(a[H].x, -a[H].y);
 }
 
 struct TwPtrs {
@@ -347,6 +374,7 @@ __global__ void __launch_bounds__(FeCfg<LOGM>::T, FeCfg<LOGM>::MIN_BLOCKS)
 
     const int n_items = a.frames * a.n_station;
     const uint32_t frame_bytes = 2u * M;
+    const int ytile_shift = __ffs(a.ytile) - 1;
     auto src_of = [&](int item) {
         const int f = item / a.n_station;
         const int s = item - f * a.n_station;
@@ -377,8 +405,8 @@ __global__ void __launch_bounds__(FeCfg<LOGM>::T, FeCfg<LOGM>::MIN_BLOCKS)
             bulk_copy_g2s(buf ? sx0 : sx1, src_of(next), frame_bytes, &bar[buf ^ 1]);
             next_issued = true;
         }
-        const YRow yrow{a.y + static_cast<size_t>(item) * kYTile,
-                        static_cast<size_t>(a.y_frames) * a.n_station * kYTile};
+        const YRow yrow{a.y + static_cast<size_t>(item) * a.ytile,
+                        static_cast<uint32_t>(a.y_frames) * a.n_station * a.ytile, ytile_shift};
 
         if (!present(item)) {
             // Missing frame: its samples count as zeros, so does its spectrum.

@@ -151,12 +151,14 @@ extern "C" corr_status corrx_accumulate_noalloc(int32_t n_station, int32_t n_fre
     fa.frames = frames;
     fa.y = d.spectra;
     fa.y_frames = frames;
+    fa.ytile = ytile_for(n_station);
     fa.err = nullptr;
     if ((st = fengine_launch(n_freq, tw, fa, d.num_sms, s)) != CORR_OK) return st;
 
     XengineArgs xa{};
     xa.y = d.spectra;
     xa.y_frames = frames;
+    xa.ytile = ytile_for(n_station);
     xa.n_station = n_station;
     xa.n_freq = n_freq;
     xa.frames = frames;

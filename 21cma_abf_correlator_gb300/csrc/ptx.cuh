@@ -97,6 +97,13 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src, uint32_t 
                  : "memory");
 }
 
+// Arrive on `bar` once every cp.async this thread issued so far has landed
+// (the arrival is not pre-counted: the barrier's count includes it).
+__device__ __forceinline__ void cp_async_mbar_arrive(uint64_t *bar) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_addr(bar))
+                 : "memory");
+}
+
 __device__ __forceinline__ void cp_async_commit() {
     asm volatile("cp.async.commit_group;" ::: "memory");
 }

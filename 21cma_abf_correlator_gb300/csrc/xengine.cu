@@ -39,9 +39,9 @@ __device__ __forceinline__ void decode_pair(int p, int nb, int *bj, int *bk) {
 }
 
 __global__ void __launch_bounds__(1024, 1)
-    xengine_plain_kernel(const float2 *__restrict__ y, int y_frames, int n_station, int npad,
-                         int n_freq, int frames, float2 *__restrict__ acc, int pairs_per_cta,
-                         int n_pairs) {
+    xengine_plain_kernel(const float2 *__restrict__ y, int y_frames, int ytile, int n_station,
+                         int npad, int n_freq, int frames, float2 *__restrict__ acc,
+                         int pairs_per_cta, int n_pairs) {
     extern __shared__ __align__(16) float2 xs[];   // [stage][frame][npad][32]
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -67,8 +67,9 @@ __global__ void __launch_bounds__(1024, 1)
             const int st = row - fi * npad;
             const int f = f0 + fi;
             const bool ok = (st < n_station) && (f < frames);
-            // two channels per 16-byte piece, inside one channel tile of the spectra
-            const float2 *src = ok ? y + y_index(c0 + part * 2, f, st, n_station, y_frames) : y;
+            // two channels per 16-byte piece, inside one channel tile
+            const float2 *src =
+                ok ? y + y_index(c0 + part * 2, f, st, n_station, y_frames, ytile) : y;
             cp_async16(dst + row * kXch + part * 2, src, ok ? 16u : 0u);
         }
     };
@@ -143,6 +144,15 @@ __global__ void scale_kernel(float2 *__restrict__ acc, size_t n, float s) {
     }
 }
 
+// One thread records the GPU's global nanosecond timer: the latency marks of a
+// captured batch (a kernel node keeps its place in the graph's order, where an
+// event recorded during capture would only express a dependency).
+__global__ void stamp_kernel(unsigned long long *slot) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    *slot = t;
+}
+
 // One thread waits on an mbarrier whose phase never completes (nothing arrives
 // on it), with a caller-chosen budget; the bounded wait gives up and records
 // kErrSelftestTimeout. The barrier is then retired by arriving on it so the CTA
@@ -188,7 +198,7 @@ corr_status xengine_plain_launch(const XengineArgs &a, int num_sms, cudaStream_t
     }
     dim3 grid(groups, a.n_freq / kXch);
     xengine_plain_kernel<<<grid, per_cta * 32, smem, stream>>>(
-        a.y, a.y_frames, a.n_station, npad, a.n_freq, a.frames, a.acc, per_cta, n_pairs);
+        a.y, a.y_frames, a.ytile, a.n_station, npad, a.n_freq, a.frames, a.acc, per_cta, n_pairs);
     return cuda_check(cudaGetLastError(), "xengine_plain_kernel launch");
 }
 
@@ -198,6 +208,11 @@ corr_status scale_launch(float2 *acc, size_t n, float s, cudaStream_t stream) {
     if (blocks > 4096) blocks = 4096;
     scale_kernel<<<static_cast<unsigned>(blocks), 256, 0, stream>>>(acc, n, s);
     return cuda_check(cudaGetLastError(), "scale_kernel launch");
+}
+
+corr_status stamp_launch(unsigned long long *slot, cudaStream_t stream) {
+    stamp_kernel<<<1, 1, 0, stream>>>(slot);
+    return cuda_check(cudaGetLastError(), "stamp_kernel launch");
 }
 
 } // namespace corrgb

@@ -21,18 +21,20 @@
 // data, so the scaled values sit in FP16's normal range and no per-channel
 // adaptive scale is needed.
 //
-// Persistent CTAs (one per SM: TMEM), 256 threads, CT channels per tile (CT/4
-// spectra tiles, each a contiguous block per stage in the channel-tiled layout):
-//   * thread 0 streams KT = 16 frames x N stations x CT channels of FP32 spectra
-//     per stage into a 3-deep shared-memory ring with 1-D TMA bulk copies
-//     (cp.async.bulk + mbarrier), running ahead across tile boundaries;
-//   * all threads convert a landed stage (scale, round, split) into the K-major
-//     no-swizzle UMMA operand layout (8-row x 16-byte core matrices), 2-deep;
-//   * thread 0 issues the stage's tcgen05.mma (M=128, N=2N rounded to 16, K=16)
-//     and commits them to the operand buffer's mbarrier;
-//   * after a tile's last stage: commit, wait, tcgen05.ld the accumulators, form
-//     V and add it into the row; the next tile's loads are already in flight.
-// Every wait is clock-bounded.
+// Warp-specialised persistent CTAs, one per SM (TMEM), CT channels per tile:
+//   control warp (lane 0): one TMA bulk copy per stage -- KT = 16 frames x N
+//     stations of one CT-channel spectra tile, a contiguous block in the
+//     channel-tiled layout -- into a ring as deep as shared memory allows (up to
+//     6 stages); tcgen05.mma issue (M=128, N=2N rounded to 16, K=16) once a
+//     stage's operands are ready; commits.
+//   8 worker warps convert a landed stage (scale, round, split) into the
+//     K-major no-swizzle UMMA operand layout (8-row x 16-byte core matrices,
+//     2-deep ring); after a tile's last stage, read the accumulators
+//     (tcgen05.ld), pair rows 2j/2j+1 with one shuffle to form V, and add V into
+//     the row with fire-and-forget reductions.
+// The roles meet only at mbarriers (stage full/empty, accumulator full/empty),
+// all waited on with clock-bounded waits, so a stuck party makes the others
+// time out and report instead of hanging.
 
 #include <algorithm>
 
@@ -44,9 +46,10 @@
 namespace corrgb {
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kWorkers = 256;                // 8 worker warps
+constexpr int kThreads = 32 + kWorkers;      // + control warp
 constexpr int kKT = 16;                      // frames per stage = one MMA K step
-constexpr int kLoadStages = 3;               // fp32 ring depth (TMA)
+constexpr int kMaxLoadStages = 6;            // fp32 ring depth (TMA), as smem allows
 constexpr int kOpStages = 2;                 // operand ring depth
 constexpr int kSBO = (kKT / 8) * 128;        // bytes per 8-row group (all K of a stage)
 constexpr int kLBO = 128;                    // bytes between K-adjacent core matrices
@@ -56,13 +59,13 @@ struct TcGeom {
     int lo_row;        // first Dl row (2N rounded up to 8); split form only
     int rows_valid;    // rows written per channel
     int n_mma;         // 2N rounded up to a multiple of 16 (MMA N, TMEM columns)
-    int ct;            // channels per tile (multiple of kYTile)
+    int ct;            // channels per tile
     int tmem_cols;     // allocated columns (power of two >= 32)
-    int chan_stride;   // operand bytes per channel (+16 B bank skew)
-    int op_stage;      // operand bytes per stage (incl. slack read by the last A)
+    int chan_stride;   // operand bytes per channel region (multiple of 128, one 128 B pad)
+    int op_stage;      // operand bytes per stage (incl. bank skew and the last A's reach)
     int ld_stage;      // fp32 bytes per stage = KT * N * CT * 8
-    int e_stride;      // floats per epilogue row
-    int epi_bytes;
+    int n_ld;          // fp32 ring depth (2..kMaxLoadStages)
+    int vs_bytes;      // epilogue staging of V
     int smem;
     bool split;
 };
@@ -75,24 +78,28 @@ TcGeom make_geom(int n_station, bool split) {
     g.rows_valid = split ? g.lo_row + 2 * n_station : 2 * n_station;
     g.n_mma = std::max(16, (2 * n_station + 15) / 16 * 16);
     int ct = 8;
-    while (ct > kYTile && ct * g.n_mma > 512) ct /= 2;
+    while (ct > 2 && ct * g.n_mma > 512) ct /= 2;
     g.ct = ct;
     int cols = 32;
     while (cols < ct * g.n_mma) cols *= 2;
     g.tmem_cols = cols;
     const int groups = (g.rows_valid + 7) / 8;
-    g.chan_stride = groups * kSBO + 16;
-    // rows read from a channel base: A reads 128 rows from Dh (and from Dl in
-    // the split form), B reads n_mma rows from the same bases
-    const int max_row = std::max((split ? g.lo_row : 0) + 128, g.rows_valid);
-    const int slack = std::max(0, (max_row + 7) / 8 * kSBO - g.chan_stride) + 128;
+    // The 128-byte pad keeps a region plus its bank skew (<= 112 B) clear of the
+    // next channel's region, whatever the skews of the two.
+    g.chan_stride = groups * kSBO + 128;
+    // A reads 128 rows from Dh (and from Dl in the split form): the last
+    // channel's reach past its own rows, plus the largest bank skew (7*16 B).
+    const int reach = ((split ? g.lo_row : 0) + 128 + 7) / 8 * kSBO;
+    const int slack = std::max(0, reach - g.chan_stride) + 7 * 16 + 128;
     g.op_stage = (g.ct * g.chan_stride + slack + 127) / 128 * 128;
     g.ld_stage = kKT * n_station * g.ct * 8;
-    g.e_stride = g.n_mma + 1;
-    const int n_baseline = n_station * (n_station + 1) / 2;
-    g.epi_bytes = (128 * g.e_stride * 4 + 15) / 16 * 16 + n_baseline * g.ct * 8;
-    // the epilogue reuses the operand ring (free once a tile's MMAs are done)
-    g.smem = kLoadStages * g.ld_stage + std::max(kOpStages * g.op_stage, g.epi_bytes) + 128;
+    g.vs_bytes = n_station * (n_station + 1) / 2 * g.ct * 8;
+    // As many TMA stages in flight as shared memory holds: the loads are rows of
+    // 8*CT bytes scattered n_freq*8 bytes apart, so latency, not bandwidth, sets
+    // how many must be outstanding.
+    const int fixed = kOpStages * g.op_stage + g.vs_bytes + 128;
+    g.n_ld = std::max(2, std::min(kMaxLoadStages, (227 * 1024 - 1024 - fixed) / g.ld_stage));
+    g.smem = g.n_ld * g.ld_stage + fixed;
     // Two CTAs on one SM would both need more than half of TMEM and the second
     // would stall in tcgen05.alloc for the first's whole (persistent) life:
     // claim more than half of shared memory so the scheduler never pairs them.
@@ -100,7 +107,14 @@ TcGeom make_geom(int n_station, bool split) {
     return g;
 }
 
-// --- tcgen05 wrappers ------------------------------------------------------
+// 16-byte bank skew of channel c's operand region: with lanes ordered (channel,
+// station), the eight 16-byte stores of a quarter warp land in eight distinct
+// slots of a 128-byte bank line for CT = 8 (one station) and CT = 4 (two).
+__host__ __device__ inline int chan_skew(int c) {
+    return ((c & 1) | ((c & 2) << 1) | ((c & 4) >> 1)) * 16;
+}
+
+// --- tcgen05 / TMA wrappers -------------------------------------------------
 
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
     // K-major, no swizzle: start>>4 | LBO>>4 << 16 | SBO>>4 << 32 | descriptor version 1 << 46
@@ -177,14 +191,23 @@ struct TcParams {
     TcGeom g;
 };
 
+struct TcBars {
+    uint64_t load_full[kMaxLoadStages];   // a stage's bulk copy landed (tx-count)
+    uint64_t op_full[kOpStages];       // workers wrote a stage's operands (256 arrivals)
+    uint64_t op_empty[kOpStages];      // MMAs reading an operand buffer finished (commit)
+    uint64_t acc_full;                 // a tile's MMAs finished (commit)
+    uint64_t acc_empty;                // workers finished reading the accumulators (256)
+    uint64_t epi;                      // worker-only sync inside the epilogue (256)
+    uint64_t fin;                      // abort path: everything this CTA issued landed
+};
+
 __global__ void __launch_bounds__(kThreads, 1) xengine_tc_kernel(TcParams p) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char *smem = smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127);
-    __shared__ uint64_t load_bar[kLoadStages];
-    __shared__ uint64_t mma_bar[kOpStages];
-    __shared__ uint64_t fin_bar;
+    __shared__ TcBars bars;
     __shared__ uint32_t s_tmem_base;
     __shared__ int s_abort;
+    __shared__ uint32_t s_ld_issued;   // bulk copies issued (abort drain)
 
     const TcGeom &g = p.g;
     const int tid = threadIdx.x;
@@ -195,20 +218,26 @@ __global__ void __launch_bounds__(kThreads, 1) xengine_tc_kernel(TcParams p) {
     const int my_tiles = (n_tiles - static_cast<int>(blockIdx.x) + static_cast<int>(gridDim.x) - 1) /
                          static_cast<int>(gridDim.x);
     const int n_stages = (p.frames + kKT - 1) / kKT;
-    const int total = my_tiles * n_stages;    // stages this CTA processes
+    const int total = my_tiles * n_stages;
     float *ld_ring = reinterpret_cast<float *>(smem);
-    unsigned char *op_ring = smem + kLoadStages * g.ld_stage;
-    const int tiles_per_ct = g.ct / kYTile;
-    const size_t ytile_stride = static_cast<size_t>(p.y_frames) * N * kYTile;   // float2
+    const int n_ld = g.n_ld;
+    unsigned char *op_ring = smem + n_ld * g.ld_stage;
+    float2 *Vs = reinterpret_cast<float2 *>(op_ring + kOpStages * g.op_stage);
 
-    // Operand rows never written (padding to 128-row blocks) must be finite.
     for (int i = tid; i < kOpStages * g.op_stage / 16; i += kThreads)
         reinterpret_cast<uint4 *>(op_ring)[i] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
-        for (int s = 0; s < kLoadStages; ++s) mbar_init(&load_bar[s], 1);
-        for (int s = 0; s < kOpStages; ++s) mbar_init(&mma_bar[s], 1);
-        mbar_init(&fin_bar, 1);
+        for (int s = 0; s < n_ld; ++s) mbar_init(&bars.load_full[s], 1);
+        for (int s = 0; s < kOpStages; ++s) {
+            mbar_init(&bars.op_full[s], kWorkers);
+            mbar_init(&bars.op_empty[s], 1);
+        }
+        mbar_init(&bars.acc_full, 1);
+        mbar_init(&bars.acc_empty, kWorkers);
+        mbar_init(&bars.epi, kWorkers);
+        mbar_init(&bars.fin, 1);
         s_abort = 0;
+        s_ld_issued = 0;
         fence_mbar_init();
     }
     if (warp == 0) {
@@ -223,190 +252,248 @@ __global__ void __launch_bounds__(kThreads, 1) xengine_tc_kernel(TcParams p) {
     tc_fence_after();
     const uint32_t tmem = s_tmem_base;
 
-    // Producer side (thread 0): load global stage gs into ring slot gs % kLoadStages.
-    auto issue_load = [&](int gs) {
-        const int tl = gs / n_stages;
-        const int st = gs - tl * n_stages;
-        const int tile = static_cast<int>(blockIdx.x) + tl * static_cast<int>(gridDim.x);
-        const int f0 = st * kKT;
-        const int nfr = min(kKT, p.y_frames - f0);
-        const uint32_t piece = static_cast<uint32_t>(nfr) * N * kYTile * 8;
-        const int slot = gs % kLoadStages;
-        float2 *dst = reinterpret_cast<float2 *>(ld_ring + slot * (g.ld_stage / 4));
-        mbar_arrive_expect_tx(&load_bar[slot], piece * tiles_per_ct);
-        for (int t = 0; t < tiles_per_ct; ++t) {
-            const int ytile = tile * tiles_per_ct + t;
-            const float2 *src = p.y + ytile * ytile_stride + static_cast<size_t>(f0) * N * kYTile;
-            bulk_copy_g2s(dst + t * (kKT * N * kYTile), src, piece, &load_bar[slot]);
-        }
+    auto tile_c0 = [&](int tl) {
+        return (static_cast<int>(blockIdx.x) + tl * static_cast<int>(gridDim.x)) * g.ct;
     };
-    if (tid == 0)
-        for (int gs = 0; gs < kLoadStages && gs < total; ++gs) issue_load(gs);
 
-    const uint32_t idesc = instr_desc_f16_f32(128, g.n_mma);
-    const int items = g.ct * N * (kKT / 8);
-    uint32_t ld_phase = 0, mma_phase = 0, fin_phase = 0;   // bit s: parity of next completion
-    const int n_baseline = N * (N + 1) / 2;
-
-    for (int gs = 0; gs < total; ++gs) {
-        const int tl = gs / n_stages;
-        const int st = gs - tl * n_stages;
-        const int c0 = (static_cast<int>(blockIdx.x) + tl * static_cast<int>(gridDim.x)) * g.ct;
-        const int lb = gs % kLoadStages;
-        const int ob = gs & 1;
-        bool ok = mbar_wait_bounded(&load_bar[lb], (ld_phase >> lb) & 1u, p.err,
-                                    kErrXengineMmaTimeout);
-        ld_phase ^= 1u << lb;
-        if (gs >= kOpStages) {
-            ok = ok && mbar_wait_bounded(&mma_bar[ob], (mma_phase >> ob) & 1u, p.err,
-                                         kErrXengineMmaTimeout);
-            mma_phase ^= 1u << ob;
+    if (warp == 0) {
+        // ------------------------------ control ------------------------------
+        if (lane == 0) {
+            // Stage gs = frames [f0, f0+KT) of this CTA's tile: one contiguous
+            // block of the spectra; frames past the buffer are left stale and
+            // zeroed by the conversion (f >= frames).
+            const size_t tile_elems = static_cast<size_t>(p.y_frames) * N * g.ct;
+            auto issue = [&](int gs) {
+                const int tl = gs / n_stages;
+                const int st = gs - tl * n_stages;
+                const int slot = gs % n_ld;
+                const int f0 = st * kKT;
+                const int nfr = min(kKT, p.y_frames - f0);
+                const uint32_t bytes = static_cast<uint32_t>(nfr) * N * g.ct * 8;
+                const int tile = tile_c0(tl) / g.ct;
+                const float2 *src = p.y + tile * tile_elems + static_cast<size_t>(f0) * N * g.ct;
+                mbar_arrive_expect_tx(&bars.load_full[slot], bytes);
+                bulk_copy_g2s(ld_ring + slot * (g.ld_stage / 4), src, bytes, &bars.load_full[slot]);
+                ++s_ld_issued;
+            };
+            for (int gs = 0; gs < n_ld && gs < total; ++gs) issue(gs);
+            const uint32_t idesc = instr_desc_f16_f32(128, g.n_mma);
+            uint32_t ph_full = 0, ph_acc_empty = 0;
+            for (int gs = 0; gs < total && !s_abort; ++gs) {
+                const int tl = gs / n_stages;
+                const int st = gs - tl * n_stages;
+                const int ob = gs & 1;
+                if (st == 0 && tl > 0) {
+                    // the previous tile's accumulators must be read before overwrite
+                    if (!mbar_wait_bounded(&bars.acc_empty, ph_acc_empty, p.err,
+                                           kErrXengineMmaTimeout)) {
+                        s_abort = 1;
+                        break;
+                    }
+                    ph_acc_empty ^= 1u;
+                }
+                if (!mbar_wait_bounded(&bars.op_full[ob], (ph_full >> ob) & 1u, p.err,
+                                       kErrXengineMmaTimeout)) {
+                    s_abort = 1;
+                    break;
+                }
+                ph_full ^= 1u << ob;
+                tc_fence_after();
+                const uint32_t base = smem_addr(op_ring + ob * g.op_stage);
+                const uint32_t acc_flag = st > 0 ? 1u : 0u;
+                for (int c = 0; c < g.ct; ++c) {
+                    const uint32_t chb = base + c * g.chan_stride + chan_skew(c);
+                    const uint32_t d = tmem + static_cast<uint32_t>(c * g.n_mma);
+                    const uint64_t hdesc = smem_desc(chb);
+                    umma_f16(d, hdesc, hdesc, idesc, acc_flag);
+                    if (g.split) {
+                        const uint64_t ldesc = smem_desc(chb + (g.lo_row / 8) * kSBO);
+                        umma_f16(d, hdesc, ldesc, idesc, 1u);
+                        umma_f16(d, ldesc, hdesc, idesc, 1u);
+                    }
+                }
+                umma_commit(&bars.op_empty[ob]);
+                if (st == n_stages - 1) umma_commit(&bars.acc_full);
+                // op_full for this stage means every worker has read its fp32
+                // slot: refill the slot n_ld stages ahead.
+                if (gs + n_ld < total) {
+                    fence_proxy_async_smem();
+                    issue(gs + n_ld);
+                }
+            }
         }
-        if (!ok) s_abort = 1;
-
-        // ld layout: [tile-in-CT][frame][station][kYTile channels]
-        const float2 *ld = reinterpret_cast<const float2 *>(ld_ring + lb * (g.ld_stage / 4));
-        unsigned char *op = op_ring + ob * g.op_stage;
-        const int f0 = st * kKT;
-        for (int q = tid; q < items; q += kThreads) {
-            const int c = q % g.ct;
-            const int rest = q / g.ct;
-            const int s = rest % N;
-            const int kq = rest / N;
-            const float2 *col = ld + (c / kYTile) * (kKT * N * kYTile) + s * kYTile + (c % kYTile);
-            uint32_t hre[4], him[4], lre[4], lim[4];
+    } else {
+        // ------------------------------ workers ------------------------------
+        const int wt = tid - 32;
+        const int items = g.ct * N * (kKT / 8);
+        const int quad = warp & 3;                 // TMEM lanes this warp may read
+        const int half = (warp - 1) >> 2;          // column-chunk parity
+        const int nchunks = g.n_mma / 16;
+        const int n_baseline = N * (N + 1) / 2;
+        uint32_t ph_load = 0, ph_empty = 0, ph_acc = 0, ph_epi = 0;
+        // Conversion: this thread's items (channel c, station s, 8-frame group kq)
+        // are also the same every stage; keep their fp32 read offsets, operand
+        // write offsets and first frame.
+        constexpr int kMaxItems = (8 * 44 * (kKT / 8) + kWorkers - 1) / kWorkers;
+        int n_item = 0;
+        uint32_t it_ld[kMaxItems], it_op[kMaxItems];
+        int it_f[kMaxItems];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const int fa = kq * 8 + 2 * i;
-                float2 va = col[fa * N * kYTile];
-                float2 vb = col[(fa + 1) * N * kYTile];
-                if (f0 + fa >= p.frames) va = make_float2(0.f, 0.f);
-                if (f0 + fa + 1 >= p.frames) vb = make_float2(0.f, 0.f);
-                const float a0 = va.x * p.scale, a1 = vb.x * p.scale;
-                const float b0 = va.y * p.scale, b1 = vb.y * p.scale;
-                const __half2 hr = __floats2half2_rn(a0, a1);
-                const __half2 hi = __floats2half2_rn(b0, b1);
-                hre[i] = half2_bits(hr);
-                him[i] = half2_bits(hi);
-                if (g.split) {
-                    const float2 fr = __half22float2(hr);
-                    const float2 fi = __half22float2(hi);
-                    lre[i] = half2_bits(__floats2half2_rn(a0 - fr.x, a1 - fr.y));
-                    lim[i] = half2_bits(__floats2half2_rn(b0 - fi.x, b1 - fi.y));
-                }
-            }
-            unsigned char *ch = op + c * g.chan_stride;
-            *reinterpret_cast<uint4 *>(ch + core_off(2 * s, kq)) =
-                make_uint4(hre[0], hre[1], hre[2], hre[3]);
-            *reinterpret_cast<uint4 *>(ch + core_off(2 * s + 1, kq)) =
-                make_uint4(him[0], him[1], him[2], him[3]);
-            if (g.split) {
-                *reinterpret_cast<uint4 *>(ch + core_off(g.lo_row + 2 * s, kq)) =
-                    make_uint4(lre[0], lre[1], lre[2], lre[3]);
-                *reinterpret_cast<uint4 *>(ch + core_off(g.lo_row + 2 * s + 1, kq)) =
-                    make_uint4(lim[0], lim[1], lim[2], lim[3]);
+        for (int i = 0; i < kMaxItems; ++i) {
+            const int q = wt + i * kWorkers;
+            if (q < items) {
+                const int c = q % g.ct;
+                const int rest = q / g.ct;
+                const int s = rest % N;
+                const int kq = rest / N;
+                it_ld[i] = static_cast<uint32_t>((kq * 8 * N + s) * g.ct + c);
+                it_op[i] = static_cast<uint32_t>(c * g.chan_stride + chan_skew(c) + core_off(2 * s, kq));
+                it_f[i] = kq * 8;
+                n_item = i + 1;
             }
         }
-        fence_proxy_async_smem();   // operand stores -> visible to the tensor cores
-        __syncthreads();
-        if (s_abort) break;
-        if (tid == 0) {
-            // the fp32 slot is consumed: refill it kLoadStages stages ahead
-            if (gs + kLoadStages < total) {
-                fence_proxy_async_smem();
-                issue_load(gs + kLoadStages);
+        const int row_step = N * g.ct;               // float2 between consecutive frames
+        const int lo_off = (g.lo_row / 8) * kSBO;    // Dl rows start here (row 2s -> lo_row + 2s)
+        for (int gs = 0; gs < total; ++gs) {
+            const int tl = gs / n_stages;
+            const int st = gs - tl * n_stages;
+            const int lb = gs % n_ld;
+            const int ob = gs & 1;
+            bool ok = mbar_wait_bounded(&bars.load_full[lb], (ph_load >> lb) & 1u, p.err,
+                                        kErrXengineMmaTimeout);
+            ph_load ^= 1u << lb;
+            if (ok && gs >= kOpStages) {
+                ok = mbar_wait_bounded(&bars.op_empty[ob], (ph_empty >> ob) & 1u, p.err,
+                                       kErrXengineMmaTimeout);
+                ph_empty ^= 1u << ob;
             }
-            tc_fence_after();
-            const uint32_t base = smem_addr(op);
-            const uint32_t acc_flag = st > 0 ? 1u : 0u;
-            for (int c = 0; c < g.ct; ++c) {
-                const uint32_t chb = base + c * g.chan_stride;
-                const uint32_t d = tmem + static_cast<uint32_t>(c * g.n_mma);
-                const uint64_t hdesc = smem_desc(chb);
-                umma_f16(d, hdesc, hdesc, idesc, acc_flag);
-                if (g.split) {
-                    const uint64_t ldesc = smem_desc(chb + (g.lo_row / 8) * kSBO);
-                    umma_f16(d, hdesc, ldesc, idesc, 1u);
-                    umma_f16(d, ldesc, hdesc, idesc, 1u);
-                }
-            }
-            umma_commit(&mma_bar[ob]);
-        }
-
-        if (st == n_stages - 1) {
-            // Tile complete: wait for all of its MMAs, then read the accumulators.
-            if (tid == 0) umma_commit(&fin_bar);
-            if (!mbar_wait_bounded(&fin_bar, fin_phase, p.err, kErrXengineMmaTimeout))
+            if (!ok) {
                 s_abort = 1;
-            fin_phase ^= 1u;
-            tc_fence_before();
-            __syncthreads();
-            tc_fence_after();
-            if (s_abort) break;
-            // Epilogue scratch aliases the operand ring: every MMA reading it is done.
-            float *E = reinterpret_cast<float *>(op_ring);
-            float2 *Vs = reinterpret_cast<float2 *>(op_ring + (128 * g.e_stride * 4 + 15) / 16 * 16);
-            const int quad = warp & 3;
-            const int half = warp >> 2;
-            const int nchunks = g.n_mma / 16;
-            for (int c = 0; c < g.ct; ++c) {
-                if (quad * 32 < 2 * N) {   // warp-uniform
-                    for (int cc = half; cc < nchunks; cc += 2) {
-                        float v[16];
-                        const uint32_t taddr = tmem + (static_cast<uint32_t>(quad * 32) << 16) +
-                                               static_cast<uint32_t>(c * g.n_mma + cc * 16);
-                        tmem_ld16(taddr, v);
-                        float *row = E + (quad * 32 + lane) * g.e_stride + cc * 16;
+                break;
+            }
+            // fp32 slot: [frame][station][CT channels]
+            const float2 *ld = reinterpret_cast<const float2 *>(ld_ring + lb * (g.ld_stage / 4));
+            unsigned char *op = op_ring + ob * g.op_stage;
+            const int f0 = st * kKT;
 #pragma unroll
-                        for (int i = 0; i < 16; ++i) row[i] = v[i];
+            for (int it = 0; it < kMaxItems; ++it) {
+                if (it >= n_item) break;
+                const float2 *src = ld + it_ld[it];
+                const int fb = f0 + it_f[it];
+                uint32_t hre[4], him[4], lre[4], lim[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    float2 va = src[(2 * i) * row_step];
+                    float2 vb = src[(2 * i + 1) * row_step];
+                    if (fb + 2 * i >= p.frames) va = make_float2(0.f, 0.f);
+                    if (fb + 2 * i + 1 >= p.frames) vb = make_float2(0.f, 0.f);
+                    const float a0 = va.x * p.scale, a1 = vb.x * p.scale;
+                    const float b0 = va.y * p.scale, b1 = vb.y * p.scale;
+                    const __half2 hr = __floats2half2_rn(a0, a1);
+                    const __half2 hi = __floats2half2_rn(b0, b1);
+                    hre[i] = half2_bits(hr);
+                    him[i] = half2_bits(hi);
+                    if (g.split) {
+                        const float2 fr = __half22float2(hr);
+                        const float2 fi = __half22float2(hi);
+                        lre[i] = half2_bits(__floats2half2_rn(a0 - fr.x, a1 - fr.y));
+                        lim[i] = half2_bits(__floats2half2_rn(b0 - fi.x, b1 - fi.y));
                     }
                 }
-                __syncthreads();
-                for (int b = tid; b < n_baseline; b += kThreads) {
-                    int j = 0, rem = b;
-                    while (rem >= N - j) {
-                        rem -= N - j;
-                        ++j;
-                    }
-                    const int k = j + rem;
-                    const float *e2j = E + (2 * j) * g.e_stride;
-                    const float *e2j1 = e2j + g.e_stride;
-                    const float re = e2j[2 * k] + e2j1[2 * k + 1];
-                    const float im = e2j1[2 * k] - e2j[2 * k + 1];
-                    Vs[b * g.ct + c] = make_float2(re * p.inv_scale2, im * p.inv_scale2);
+                unsigned char *dst = op + it_op[it];
+                *reinterpret_cast<uint4 *>(dst) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
+                *reinterpret_cast<uint4 *>(dst + 16) = make_uint4(him[0], him[1], him[2], him[3]);
+                if (g.split) {
+                    *reinterpret_cast<uint4 *>(dst + lo_off) =
+                        make_uint4(lre[0], lre[1], lre[2], lre[3]);
+                    *reinterpret_cast<uint4 *>(dst + lo_off + 16) =
+                        make_uint4(lim[0], lim[1], lim[2], lim[3]);
                 }
-                __syncthreads();
             }
-            for (int q = tid; q < n_baseline * g.ct; q += kThreads) {
-                const int b = q / g.ct;
-                const int c = q - b * g.ct;
-                float2 *dst = p.acc + static_cast<size_t>(b) * p.n_freq + c0 + c;
-                float2 a = *dst;
-                const float2 v = Vs[q];
-                a.x += v.x;
-                a.y += v.y;
-                *dst = a;
+            fence_proxy_async_smem();   // operand stores -> visible to the tensor cores
+            mbar_arrive(&bars.op_full[ob]);
+
+            if (st == n_stages - 1) {
+                // ---- epilogue of tile tl ----
+                if (!mbar_wait_bounded(&bars.acc_full, ph_acc, p.err, kErrXengineMmaTimeout)) {
+                    s_abort = 1;
+                    break;
+                }
+                ph_acc ^= 1u;
+                tc_fence_after();
+                // TMEM lane m holds row m of S; lanes 2j and 2j+1 are neighbours,
+                // so one shfl_down gives lane 2j the four terms of V[j][k].
+                const int m = quad * 32 + lane;
+                const int j = m >> 1;
+                const bool row_lane = ((lane & 1) == 0) && (m < 2 * N);
+                if (quad * 32 < 2 * N) {            // warp-uniform
+                    for (int c = 0; c < g.ct; ++c) {
+                        for (int cc = half; cc < nchunks; cc += 2) {
+                            float v[16], w[16];
+                            tmem_ld16(tmem + (static_cast<uint32_t>(quad * 32) << 16) +
+                                          static_cast<uint32_t>(c * g.n_mma + cc * 16),
+                                      v);
+#pragma unroll
+                            for (int i = 0; i < 16; ++i) w[i] = __shfl_down_sync(0xffffffffu, v[i], 1);
+                            if (row_lane) {
+#pragma unroll
+                                for (int t = 0; t < 8; ++t) {
+                                    const int k = cc * 8 + t;
+                                    if (k >= j && k < N) {
+                                        // v = S[2j][*], w = S[2j+1][*]
+                                        const float re = v[2 * t] + w[2 * t + 1];
+                                        const float im = w[2 * t] - v[2 * t + 1];
+                                        const int b = j * N - j * (j - 1) / 2 + (k - j);
+                                        Vs[b * g.ct + c] =
+                                            make_float2(re * p.inv_scale2, im * p.inv_scale2);
+                                    }
+                                }
+                            }
+                        }
+                    }
+                }
+                // accumulators read: the control warp may start the next tile
+                tc_fence_before();
+                mbar_arrive(&bars.acc_empty);
+                // all of V staged before anyone reads it back
+                mbar_arrive(&bars.epi);
+                if (!mbar_wait_bounded(&bars.epi, ph_epi, p.err, kErrXengineMmaTimeout)) {
+                    s_abort = 1;
+                    break;
+                }
+                ph_epi ^= 1u;
+                const int c0 = tile_c0(tl);
+                // one owner per (baseline, channel) in this launch: fire-and-forget adds
+                for (int q = wt; q < n_baseline * g.ct; q += kWorkers) {
+                    const int b = q / g.ct;
+                    const int c = q - b * g.ct;
+                    float *dst = reinterpret_cast<float *>(
+                        p.acc + static_cast<size_t>(b) * p.n_freq + c0 + c);
+                    const float2 v = Vs[q];
+                    atomicAdd(dst, v.x);
+                    atomicAdd(dst + 1, v.y);
+                }
             }
-            // The next tile's first conversion overwrites the operand ring (and the
-            // next MMA the accumulators): everyone must be past the epilogue.
-            tc_fence_before();
-            __syncthreads();
-            tc_fence_after();
         }
     }
 
-    if (s_abort) {
-        // Let every MMA and bulk copy this CTA started land before TMEM and the
-        // CTA go away.
-        if (tid == 0) {
-            umma_commit(&fin_bar);
-            mbar_wait_bounded(&fin_bar, fin_phase, nullptr, 0);
-            for (int s = 0; s < kLoadStages; ++s)
-                mbar_wait_bounded(&load_bar[s], (ld_phase >> s) & 1u, nullptr, 0);
+    tc_fence_before();
+    __syncthreads();
+    if (s_abort && tid == 0) {
+        // Let every MMA and bulk copy this CTA issued land before TMEM and the
+        // CTA go away (bounded; the watchdog code is already recorded). A slot
+        // whose copy was consumed completed its phase; one still in flight
+        // completes the phase after the last one consumed.
+        umma_commit(&bars.fin);
+        mbar_wait_bounded(&bars.fin, 0u, nullptr, 0);
+        for (int s = 0; s < n_ld; ++s) {
+            // copies issued into slot s (round robin from stage 0); the last
+            // one's completion is phase n_s - 1 of that slot's barrier
+            const uint32_t n_s = (s_ld_issued + n_ld - 1 - s) / n_ld;
+            if (n_s > 0) mbar_wait_bounded(&bars.load_full[s], (n_s - 1) & 1u, nullptr, 0);
         }
-        tc_fence_before();
-        __syncthreads();
     }
+    __syncthreads();
     if (warp == 0) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
@@ -435,6 +522,9 @@ corr_status xengine_tc_launch(const XengineArgs &a, bool split, int num_sms,
         return failf(CORR_ERR_ARG, "n_freq=%d is not a multiple of %d channels", a.n_freq, g.ct);
     if (a.y_frames < a.frames)
         return fail(CORR_ERR_INTERNAL, "spectra buffer shallower than the launch");
+    if (a.ytile != g.ct)
+        return failf(CORR_ERR_INTERNAL, "spectra tiles of %d channels, tensor engine tiles of %d",
+                     a.ytile, g.ct);
     static int configured_smem = 0;
     if (configured_smem < g.smem) {
         corr_status st = cuda_check(

@@ -12,6 +12,11 @@ are generated in HBM before timing and are larger than L2, so no flush is needed
   roofline   : the dominant kernel's achieved algorithmic bytes/s vs measured HBM
   cpu_baseline: the numpy float64 oracle (the reference's gen_golden.py
                formulation) on a bounded sample, on this host's cores
+  batching   : 64 integration blocks of 512..8192 frames (24 inputs, n_freq 16384,
+               0.5% packet loss, pooled 8192-frame ring) in one CUDA-graph launch:
+               aggregate GS/s and per-block latency p50/p99
+  stream     : 40 inputs, n_freq 16384, 4096-frame integrations with the split
+               tensor X-engine: GS/s and the real-time factor against 40 x 250 MS/s
 
 --impl reference runs the reference's CPU formulation of the path (the oracle
 port, multi-process over all host cores) on the same workload and metric.
@@ -37,7 +42,7 @@ REPO = Path(__file__).resolve().parent
 sys.path.insert(0, str(REPO))
 PKG_NAME = "21cma_abf_correlator_gb300"
 METRIC = "fused F+X GSample/s"
-MAX_FRAMES = 256
+PASS_FRAMES = 512         # default frames per F/X pass on the device-resident path
 
 
 def peaks():
@@ -185,6 +190,7 @@ def run_reference(args) -> None:
 
 
 def main() -> None:
+    global PASS_FRAMES
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -197,7 +203,12 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--frames", type=int, default=0,
                     help="override frames per integration (smaller cases for profiling)")
+    ap.add_argument("--pass-frames", type=int, default=PASS_FRAMES,
+                    help="frames per F/X pass (spectra buffer depth)")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the batching and stream workloads")
     args = ap.parse_args()
+    PASS_FRAMES = args.pass_frames
     args.warmup = max(args.warmup, 3)
 
     if args.impl == "reference":
@@ -249,7 +260,7 @@ def main() -> None:
     engines = {}
     for name in candidates:
         try:
-            eng = pkg.FxEngine(N, nf, MAX_FRAMES, xmode=modes[name])
+            eng = pkg.FxEngine(N, nf, PASS_FRAMES, xmode=modes[name])
             acc = eng.new_acc()
             step = make_step(eng, acc)
             step()
@@ -305,7 +316,7 @@ def main() -> None:
         m = ms if name == best else time_steps(s_, max(2, args.steps // 2), 1)
         paths[name] = {"value": samples_step / (m * 1e-3) / 1e9, "ms_per_step": m}
 
-    # per-kernel times: one pass of MAX_FRAMES frames through each kernel alone
+    # per-kernel times: one pass of PASS_FRAMES frames through each kernel alone
     hbm_peak, _, peak_kind = peaks()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     reps = 8
@@ -313,21 +324,21 @@ def main() -> None:
         abi.check(eng.lib.corrx_run_fengine(eng.h, x.data_ptr(), x.stride(0), x.stride(1),
                                             mask.data_ptr() if mask is not None else None,
                                             mask.stride(0) if mask is not None else 0, 0,
-                                            MAX_FRAMES, stream.cuda_stream), "fengine")
-        abi.check(eng.lib.corrx_run_xengine(eng.h, MAX_FRAMES, acc.data_ptr(),
+                                            PASS_FRAMES, stream.cuda_stream), "fengine")
+        abi.check(eng.lib.corrx_run_xengine(eng.h, PASS_FRAMES, acc.data_ptr(),
                                             stream.cuda_stream), "xengine")
     torch.cuda.synchronize()
     t_f = t_x = 0.0
     for r in range(reps):
-        f0 = (r * MAX_FRAMES) % (F - MAX_FRAMES + 1)
+        f0 = (r * PASS_FRAMES) % (F - PASS_FRAMES + 1)
         base = x.data_ptr() + f0 * x.stride(1)
         ev[0].record(stream)
         abi.check(eng.lib.corrx_run_fengine(eng.h, base, x.stride(0), x.stride(1),
                                             mask.data_ptr() if mask is not None else None,
                                             mask.stride(0) if mask is not None else 0, f0,
-                                            MAX_FRAMES, stream.cuda_stream), "fengine")
+                                            PASS_FRAMES, stream.cuda_stream), "fengine")
         ev[1].record(stream)
-        abi.check(eng.lib.corrx_run_xengine(eng.h, MAX_FRAMES, acc.data_ptr(),
+        abi.check(eng.lib.corrx_run_xengine(eng.h, PASS_FRAMES, acc.data_ptr(),
                                             stream.cuda_stream), "xengine")
         ev[2].record(stream)
         torch.cuda.synchronize()
@@ -336,32 +347,43 @@ def main() -> None:
     t_f /= reps
     t_x /= reps
     mb = synth.mask_bytes(F) if mask is not None else 0
-    f_bytes = N * MAX_FRAMES * L + N * MAX_FRAMES * nf * 8 + (N * mb * MAX_FRAMES // F)
-    x_bytes = N * MAX_FRAMES * nf * 8 + 2 * B * nf * 8
+    f_bytes = N * PASS_FRAMES * L + N * PASS_FRAMES * nf * 8 + (N * mb * PASS_FRAMES // F)
+    x_bytes = N * PASS_FRAMES * nf * 8 + 2 * B * nf * 8
     kernels = {
         "fengine": {"ms_per_launch": t_f, "alg_bytes": f_bytes,
                     "achieved_gbs": f_bytes / (t_f * 1e-3) / 1e9},
         "xengine_" + best: {"ms_per_launch": t_x, "alg_bytes": x_bytes,
                             "achieved_gbs": x_bytes / (t_x * 1e-3) / 1e9,
-                            "alg_tflops": 8.0 * B * nf * MAX_FRAMES / (t_x * 1e-3) / 1e12},
+                            "alg_tflops": 8.0 * B * nf * PASS_FRAMES / (t_x * 1e-3) / 1e12},
     }
     dom = "fengine" if t_f >= t_x else "xengine_" + best
     dk = kernels[dom]
     roofline = {"kernel": dom, "bound": "hbm", "achieved": dk["achieved_gbs"],
                 "peak": hbm_peak, "unit": "GB/s", "frac": dk["achieved_gbs"] / hbm_peak,
                 "peak_kind": peak_kind, "traffic": None,
-                "alg_bytes_per_launch": dk["alg_bytes"], "frames_per_launch": MAX_FRAMES}
+                "alg_bytes_per_launch": dk["alg_bytes"], "frames_per_launch": PASS_FRAMES}
 
     e2e = None
     if not args.no_e2e and rank == 0:
         e2e = run_e2e(pkg, w, x, mask, modes[best], args, torch)
+
+    extra = {}
+    if not args.no_extra and rank == 0 and not args.frames:
+        for e_ in engines.values():
+            e_[0].close()
+        del x, mask
+        torch.cuda.empty_cache()
+        extra["batching"] = run_batching(pkg, synth, torch, modes[best], stream)
+        torch.cuda.empty_cache()
+        extra["stream"] = run_stream(pkg, synth, torch, stream)
+        torch.cuda.empty_cache()
 
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         cpu = time_cpu_oracle(w, args.cpu_seconds, 1)
         cpu["kind"] = "port"
 
-    passes = math.ceil(F / MAX_FRAMES)
+    passes = math.ceil(F / PASS_FRAMES)
     launches_per_step = 2 * passes + 1
     if rank == 0:
         line = {
@@ -372,15 +394,93 @@ def main() -> None:
             "data": "synthetic (seeded Gaussian + common signal, delays; generated in HBM)",
             "config": {"workload": w.name, "n_station": N, "n_freq": nf,
                        "frames_per_integration": F, "baselines": B, "xengine": best,
-                       "frames_per_pass": MAX_FRAMES, "parallelism": f"replicas x{world}",
+                       "frames_per_pass": PASS_FRAMES, "parallelism": f"replicas x{world}",
                        "l2": f"inputs {N * F * L / 1e9:.2f} GB per step > L2; no flush"},
             "paths": paths, "kernels": kernels, "roofline": roofline,
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
             "gpu_launches": launches_per_step * args.steps,
         }
+        line.update(extra)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_batching(pkg, synth, torch, xmode, stream) -> dict:
+    """64 uneven integration blocks captured in one CUDA graph (corrx_batch_*)."""
+    import ctypes as C
+    abi = pkg.abi
+    w = synth.WORKLOADS["batching-24in-nf16384"]
+    pool, mask = synth.generate_torch(w, w.frames)            # 8192-frame ring
+    plan = synth.block_plan(w)
+    nblk = len(plan)
+    eng = pkg.FxEngine(w.n_station, w.n_freq, PASS_FRAMES, xmode=xmode)
+    rows = torch.empty((nblk, w.n_baseline, w.n_freq), dtype=torch.complex64, device="cuda")
+    host = torch.empty((nblk, w.n_baseline, w.n_freq), dtype=torch.complex64).pin_memory()
+    first = (C.c_int64 * nblk)(*[b[0] for b in plan])
+    frames = (C.c_int32 * nblk)(*[b[1] for b in plan])
+    h = C.c_void_p()
+    abi.check(eng.lib.corrx_batch_create(
+        eng.h, C.c_void_p(pool.data_ptr()), pool.stride(0), pool.stride(1),
+        C.c_void_p(mask.data_ptr()), mask.stride(0), first, frames, nblk,
+        C.c_void_p(rows.data_ptr()), C.c_void_p(host.data_ptr()), C.byref(h)),
+        "corrx_batch_create")
+    try:
+        abi.check(eng.lib.corrx_batch_launch(h, C.c_void_p(stream.cuda_stream)), "launch")
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        abi.check(eng.lib.corrx_batch_launch(h, C.c_void_p(stream.cuda_stream)), "launch")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        eng.check()
+        ms = e0.elapsed_time(e1)
+        lat = (C.c_float * nblk)()
+        abi.check(eng.lib.corrx_batch_block_ms(h, lat, nblk), "corrx_batch_block_ms")
+    finally:
+        eng.lib.corrx_batch_destroy(h)
+        eng.close()
+    total_frames = sum(b[1] for b in plan)
+    samples = w.n_station * total_frames * w.fft_len
+    lat = np.array(list(lat))
+    return {"workload": w.name, "blocks": nblk, "frames_total": total_frames,
+            "value": samples / (ms * 1e-3) / 1e9, "unit": "GSample/s", "ms_per_launch": ms,
+            "graph_launches": 1, "latency_ms": {"p50": float(np.percentile(lat, 50)),
+                                                "p99": float(np.percentile(lat, 99)),
+                                                "max": float(lat.max())},
+            "latency": "block start to its row in pinned host memory, inside the graph"}
+
+
+def run_stream(pkg, synth, torch, stream) -> dict:
+    """40 inputs at 250 MS/s each: one 4096-frame integration with the split engine."""
+    w = synth.WORKLOADS["stream-40in-nf16384"]
+    x, mask = synth.generate_torch(w, w.frames)
+    eng = pkg.FxEngine(w.n_station, w.n_freq, PASS_FRAMES,
+                       xmode=pkg.abi.CORR_X_TC_FP16_SPLIT)
+    acc = eng.new_acc()
+
+    def step():
+        acc.zero_()
+        eng.accumulate(x, w.frames, acc, mask=mask, stream=stream)
+        eng.scale(acc, w.frames, stream=stream)
+    for _ in range(2):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(2):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    eng.check()
+    ms = e0.elapsed_time(e1) / 2
+    eng.close()
+    gs = w.n_station * w.frames * w.fft_len / (ms * 1e-3) / 1e9
+    need = w.n_station * 0.25
+    return {"workload": w.name, "xengine": "tc_split", "value": gs, "unit": "GSample/s",
+            "ms_per_integration": ms, "real_time_factor": gs / need,
+            "real_time_need_gsps": need,
+            "integrations_per_60s": 60.0 * 250e6 / (w.frames * w.fft_len)}
 
 
 def run_e2e(pkg, w, x, mask, xmode, args, torch) -> dict:

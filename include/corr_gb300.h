@@ -88,6 +88,33 @@ corr_status corrx_run_xengine(void *eng, int32_t frames, void *d_acc, void *stre
 corr_status corrx_selftest_watchdog(void *eng, int64_t budget_cycles, void *stream);
 
 /*
+ * Batched integration blocks in one CUDA graph. No counterpart in the reference
+ * (whose host drives one row at a time through corr_row_accumulate/row_end).
+ *
+ * corrx_batch_create captures, for every block i, the whole life of one
+ * integration into a single graph:
+ *   clear row i of d_rows (n_baseline*n_freq complex64 per block)
+ *   F/X passes over frames [block_first[i], block_first[i] + block_frames[i])
+ *   scale by 1/block_frames[i]
+ *   copy row i to h_rows (pinned host, may be NULL) on a side stream
+ * with a GPU timestamp at each block's start and after its dump.
+ * corrx_batch_launch replays the graph on `stream` (one launch for all blocks);
+ * corrx_batch_block_ms waits for the last launch and reports each block's
+ * latency from its start to its row being on the host (or computed, without
+ * h_rows); CORR_ERR_STATE before any launch. block_first/block_frames are host arrays
+ * read at creation; samples/mask follow corrx_accumulate's conventions and must
+ * stay valid for the batch's lifetime.
+ */
+corr_status corrx_batch_create(void *eng, const int8_t *d_samples, size_t station_stride,
+                               size_t frame_stride, const uint8_t *d_mask,
+                               size_t mask_station_stride, const int64_t *block_first,
+                               const int32_t *block_frames, int32_t n_blocks, void *d_rows,
+                               void *h_rows, void **out_batch);
+corr_status corrx_batch_launch(void *batch, void *stream);
+corr_status corrx_batch_block_ms(void *batch, float *out_ms, int32_t n);
+corr_status corrx_batch_destroy(void *batch);
+
+/*
  * corrx_accumulate without any device allocation. No counterpart in the
  * reference. For callers that may not call cudaMalloc (a host that owns all
  * device memory through its own pool, code inside stream capture or a
