@@ -101,6 +101,17 @@ class corrx_params(C.Structure):
     ]
 
 
+class corrx_tiles(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_uint32),
+        ("ytile", C.c_int32),
+        ("xct", C.c_int32),
+        ("xkt", C.c_int32),
+        ("ms_fengine", C.c_float),
+        ("ms_xengine", C.c_float),
+    ]
+
+
 # Layouts pinned by the reference's Rust mirror (ffi.rs compile-time asserts).
 assert C.sizeof(corr_config) == 76
 assert C.sizeof(corr_device_plan) == 20
@@ -146,6 +157,10 @@ SIGNATURES = {
                                    C.c_size_t, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "corrx_scale": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "corrx_check": (C.c_int, [C.c_void_p]),
+    "corrx_get_tiles": (C.c_int, [C.c_void_p, C.POINTER(corrx_tiles)]),
+    "corrx_set_tiles": (C.c_int, [C.c_void_p, C.POINTER(corrx_tiles)]),
+    "corrx_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(corrx_tiles)]),
+    "corr_autotune": (C.c_int, [C.c_void_p, C.POINTER(corrx_tiles)]),
     "corrx_run_fengine": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p,
                                     C.c_size_t, C.c_int32, C.c_int32, C.c_void_p]),
     "corrx_run_xengine": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),

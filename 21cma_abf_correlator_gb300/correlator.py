@@ -138,6 +138,13 @@ class Correlator:
     def set_xengine(self, mode: int) -> None:
         abi.check(self.lib.corr_set_xengine(self.ctx, mode), "corr_set_xengine")
 
+    def autotune(self) -> dict:
+        """Pick the fastest spectra layout and tensor X tile for this context's engine."""
+        t = abi.corrx_tiles(struct_size=C.sizeof(abi.corrx_tiles))
+        abi.check(self.lib.corr_autotune(self.ctx, C.byref(t)), "corr_autotune")
+        return {"ytile": t.ytile, "xct": t.xct, "xkt": t.xkt,
+                "ms_fengine": t.ms_fengine, "ms_xengine": t.ms_xengine}
+
     def stats(self) -> abi.corr_device_stats:
         st = abi.corr_device_stats()
         abi.check(self.lib.corr_device_stats_get(self.ctx, 0, C.byref(st)), "corr_device_stats_get")

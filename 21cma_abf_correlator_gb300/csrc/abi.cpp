@@ -736,6 +736,28 @@ extern "C" corr_status corr_set_xengine(void *h, int32_t mode) {
         return fail(CORR_ERR_STATE,
                     "the X-engine can only change while no row holds data (after create or a "
                     "fetch)");
+    if (mode != CORR_X_PLAIN_FP32) {
+        int ct = 0, kt = 0;
+        corrgb::xengine_tc_default_shape(c->plan->n_station, mode == CORR_X_TC_FP16_SPLIT, &ct, &kt);
+        if (ct == 0)
+            return failf(CORR_ERR_NOT_IMPL, "the tensor X-engine takes 1..64 inputs (n_station=%d)",
+                         c->plan->n_station);
+        c->plan->xct = ct;
+        c->plan->xkt = kt;
+        if (c->plan->ytile < ct) c->plan->ytile = c->plan->n_freq;
+    }
     c->plan->xmode = mode;
     return CORR_OK;
+}
+
+extern "C" corr_status corr_autotune(void *h, corrx_tiles *out) {
+    Context *c = as_ctx(h);
+    if (c == nullptr) return fail(CORR_ERR_ARG, "ctx is NULL");
+    if (out != nullptr && out->struct_size != sizeof(corrx_tiles))
+        return failf(CORR_ERR_ABI, "corrx_tiles.struct_size=%u, expected %zu", out->struct_size,
+                     sizeof(corrx_tiles));
+    if (c->dirty || c->pending != 0)
+        return fail(CORR_ERR_STATE,
+                    "tiles can only be tuned while no row holds data (after create or a fetch)");
+    return corrgb::fxplan_autotune(c->plan, c->s_compute, out);
 }

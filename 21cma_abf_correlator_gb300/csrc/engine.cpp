@@ -88,8 +88,16 @@ corr_status fxplan_create(int device, int n_station, int n_freq, int max_frames,
     p->n_freq = n_freq;
     p->n_baseline = n_station * (n_station + 1) / 2;
     p->max_frames = max_frames;
-    p->ytile = ytile_for(n_station);
+    p->ytile = n_freq;
     p->xmode = xmode;
+    if (xmode != CORR_X_PLAIN_FP32) {
+        xengine_tc_default_shape(n_station, xmode == CORR_X_TC_FP16_SPLIT, &p->xct, &p->xkt);
+        if (p->xct == 0) {
+            delete p;
+            return failf(CORR_ERR_NOT_IMPL, "the tensor X-engine takes 1..64 inputs (n_station=%d)",
+                         n_station);
+        }
+    }
     if ((st = cuda_check(cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount,
                                                 device),
                          "cudaDeviceGetAttribute(SM count)")) != CORR_OK) {
@@ -164,7 +172,8 @@ corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_s
         if (p->xmode == CORR_X_PLAIN_FP32)
             st = xengine_plain_launch(xa, p->num_sms, stream);
         else
-            st = xengine_tc_launch(xa, p->xmode == CORR_X_TC_FP16_SPLIT, p->num_sms, stream);
+            st = xengine_tc_launch(xa, p->xmode == CORR_X_TC_FP16_SPLIT, p->xct, p->xkt,
+                                   p->num_sms, stream);
         if (st != CORR_OK) return st;
     }
     return CORR_OK;
@@ -294,8 +303,171 @@ extern "C" corr_status corrx_run_xengine(void *eng, int32_t frames, void *d_acc,
     xa.err = p->d_err;
     if (p->xmode == CORR_X_PLAIN_FP32)
         return xengine_plain_launch(xa, p->num_sms, static_cast<cudaStream_t>(stream));
-    return xengine_tc_launch(xa, p->xmode == CORR_X_TC_FP16_SPLIT, p->num_sms,
+    return xengine_tc_launch(xa, p->xmode == CORR_X_TC_FP16_SPLIT, p->xct, p->xkt, p->num_sms,
                              static_cast<cudaStream_t>(stream));
+}
+
+// ---------------------------------------------------------------------------
+// Tile shapes and the autotuner.
+// ---------------------------------------------------------------------------
+
+namespace corrgb {
+
+corr_status fxplan_set_tiles(FxPlan *p, int ytile, int xct, int xkt) {
+    if (ytile < 2 || ytile > p->n_freq || (ytile & (ytile - 1)) != 0)
+        return failf(CORR_ERR_ARG, "ytile=%d is not a power of two in [2, n_freq=%d]", ytile,
+                     p->n_freq);
+    if (p->xmode != CORR_X_PLAIN_FP32) {
+        if (!xengine_tc_shape_ok(p->n_station, p->xmode == CORR_X_TC_FP16_SPLIT, xct, xkt))
+            return failf(CORR_ERR_ARG,
+                         "no tensor X-engine tile of %d channels x %d frames for %d inputs", xct,
+                         xkt, p->n_station);
+        if (ytile < xct)
+            return failf(CORR_ERR_ARG, "ytile=%d is narrower than the tensor tile (%d channels)",
+                         ytile, xct);
+        p->xct = xct;
+        p->xkt = xkt;
+    }
+    p->ytile = ytile;
+    return CORR_OK;
+}
+
+corr_status fxplan_autotune(FxPlan *p, cudaStream_t stream, corrx_tiles *out) {
+    corr_status st = cuda_check(cudaSetDevice(p->device), "cudaSetDevice");
+    if (st != CORR_OK) return st;
+    struct Cand {
+        int ytile, ct, kt;
+    };
+    std::vector<Cand> cands;
+    if (p->xmode == CORR_X_PLAIN_FP32) {
+        cands.push_back({p->n_freq, p->xct, p->xkt});
+    } else {
+        const bool split = p->xmode == CORR_X_TC_FP16_SPLIT;
+        for (int ct = 8; ct >= 2; ct /= 2)
+            for (int kt = 16; kt <= 32; kt *= 2)
+                if (xengine_tc_shape_ok(p->n_station, split, ct, kt)) {
+                    cands.push_back({p->n_freq, ct, kt});
+                    if (ct < p->n_freq) cands.push_back({ct, ct, kt});
+                }
+    }
+    if (cands.empty()) return fail(CORR_ERR_INTERNAL, "autotune: no candidate tile");
+    const int frames = std::min(p->max_frames, 1024);
+    const int L = 2 * p->n_freq;
+    const size_t x_bytes = static_cast<size_t>(p->n_station) * frames * L;
+    const size_t acc_bytes = static_cast<size_t>(p->n_baseline) * p->n_freq * sizeof(float2);
+    int8_t *d_x = nullptr;
+    float2 *d_acc = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    const int ytile0 = p->ytile, ct0 = p->xct, kt0 = p->xkt;
+    auto cleanup = [&] {
+        if (d_x) cudaFree(d_x);
+        if (d_acc) cudaFree(d_acc);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+    if ((st = cuda_check(cudaMalloc(&d_x, x_bytes), "cudaMalloc(autotune frames)")) != CORR_OK ||
+        (st = cuda_check(cudaMalloc(&d_acc, acc_bytes), "cudaMalloc(autotune row)")) != CORR_OK ||
+        (st = cuda_check(cudaEventCreate(&e0), "cudaEventCreate")) != CORR_OK ||
+        (st = cuda_check(cudaEventCreate(&e1), "cudaEventCreate")) != CORR_OK ||
+        (st = synth_fill_launch(d_x, x_bytes, 0x2c1bu, stream)) != CORR_OK ||
+        (st = cuda_check(cudaMemsetAsync(d_acc, 0, acc_bytes, stream), "cudaMemsetAsync")) !=
+            CORR_OK) {
+        cleanup();
+        return st;
+    }
+    // time one launch of `run` (after one untimed launch): best of two
+    auto timed = [&](auto &&run, float *ms) -> corr_status {
+        corr_status s2 = run();
+        float best = 1e30f;
+        for (int r = 0; r < 2 && s2 == CORR_OK; ++r) {
+            if ((s2 = cuda_check(cudaEventRecord(e0, stream), "cudaEventRecord")) != CORR_OK) break;
+            if ((s2 = run()) != CORR_OK) break;
+            if ((s2 = cuda_check(cudaEventRecord(e1, stream), "cudaEventRecord")) != CORR_OK) break;
+            if ((s2 = cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize")) != CORR_OK) break;
+            float t = 0.f;
+            if ((s2 = cuda_check(cudaEventElapsedTime(&t, e0, e1), "cudaEventElapsedTime")) !=
+                CORR_OK)
+                break;
+            best = std::min(best, t);
+        }
+        *ms = best;
+        return s2;
+    };
+    auto run_f = [&] {
+        return corrx_run_fengine(p, d_x, static_cast<size_t>(frames) * L, L, nullptr, 0, 0, frames,
+                                 stream);
+    };
+    auto run_x = [&] { return corrx_run_xengine(p, frames, d_acc, stream); };
+    float best_total = 1e30f, best_f = 0.f, best_x = 0.f;
+    Cand best{ytile0, ct0, kt0};
+    int f_ytile = -1;
+    float f_ms = 0.f;
+    for (const Cand &c : cands) {
+        if ((st = fxplan_set_tiles(p, c.ytile, c.ct, c.kt)) != CORR_OK) break;
+        if (c.ytile != f_ytile) {   // the F-engine depends on the layout only
+            if ((st = timed(run_f, &f_ms)) != CORR_OK) break;
+            f_ytile = c.ytile;
+        } else if ((st = run_f()) != CORR_OK) {
+            break;
+        }
+        float x_ms = 0.f;
+        if ((st = timed(run_x, &x_ms)) != CORR_OK) break;
+        if (f_ms + x_ms < best_total) {
+            best_total = f_ms + x_ms;
+            best = c;
+            best_f = f_ms;
+            best_x = x_ms;
+        }
+    }
+    corr_status st_check = st == CORR_OK ? fxplan_check(p) : st;
+    cleanup();
+    if (st_check != CORR_OK) {
+        fxplan_set_tiles(p, ytile0, ct0, kt0);
+        return st_check;
+    }
+    if ((st = fxplan_set_tiles(p, best.ytile, best.ct, best.kt)) != CORR_OK) return st;
+    if (out != nullptr) {
+        out->ytile = p->ytile;
+        out->xct = p->xct;
+        out->xkt = p->xkt;
+        out->ms_fengine = best_f;
+        out->ms_xengine = best_x;
+    }
+    return CORR_OK;
+}
+
+} // namespace corrgb
+
+extern "C" corr_status corrx_get_tiles(void *eng, corrx_tiles *out) {
+    FxPlan *p = static_cast<FxPlan *>(eng);
+    if (p == nullptr || out == nullptr) return fail(CORR_ERR_ARG, "eng and out must be non-NULL");
+    if (out->struct_size != sizeof(corrx_tiles))
+        return failf(CORR_ERR_ABI, "corrx_tiles.struct_size=%u, expected %zu", out->struct_size,
+                     sizeof(corrx_tiles));
+    out->ytile = p->ytile;
+    out->xct = p->xct;
+    out->xkt = p->xkt;
+    out->ms_fengine = 0.f;
+    out->ms_xengine = 0.f;
+    return CORR_OK;
+}
+
+extern "C" corr_status corrx_set_tiles(void *eng, const corrx_tiles *t) {
+    FxPlan *p = static_cast<FxPlan *>(eng);
+    if (p == nullptr || t == nullptr) return fail(CORR_ERR_ARG, "eng and t must be non-NULL");
+    if (t->struct_size != sizeof(corrx_tiles))
+        return failf(CORR_ERR_ABI, "corrx_tiles.struct_size=%u, expected %zu", t->struct_size,
+                     sizeof(corrx_tiles));
+    return fxplan_set_tiles(p, t->ytile, t->xct, t->xkt);
+}
+
+extern "C" corr_status corrx_autotune(void *eng, void *stream, corrx_tiles *out) {
+    FxPlan *p = static_cast<FxPlan *>(eng);
+    if (p == nullptr) return fail(CORR_ERR_ARG, "eng is NULL");
+    if (out != nullptr && out->struct_size != sizeof(corrx_tiles))
+        return failf(CORR_ERR_ABI, "corrx_tiles.struct_size=%u, expected %zu", out->struct_size,
+                     sizeof(corrx_tiles));
+    return fxplan_autotune(p, static_cast<cudaStream_t>(stream), out);
 }
 
 extern "C" corr_status corrx_selftest_watchdog(void *eng, int64_t budget_cycles, void *stream) {

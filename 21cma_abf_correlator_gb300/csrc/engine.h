@@ -54,23 +54,16 @@ struct TwiddleTables {
 };
 
 /// Spectra layout shared by the F- and X-engines: channel tiles of `ytile`
-/// channels (a power of two), each tile holding every frame and station,
+/// channels (a power of two in [2, n_freq]), each tile holding every frame and
+/// station,
 ///   y[((c / ytile) * y_frames + f) * n_station + s) * ytile + c % ytile]
-/// ytile is the tensor X-engine's channels per CTA, so the KT frames x N
-/// stations of one tile that a CTA consumes per stage are one contiguous block
-/// (one bulk copy), while a warp of the F-engine still writes whole 32-byte
-/// sectors (32 consecutive bins = 32/ytile pieces of ytile*8 bytes).
+/// ytile = n_freq is one contiguous row of n_freq bins per (frame, station)
+/// (the F-engine's cheapest store pattern); ytile equal to the tensor
+/// X-engine's channels per tile makes each of its stages one contiguous block.
 __host__ __device__ inline size_t y_index(int c, int f, int s, int n_station, int y_frames,
                                           int ytile) {
     return ((static_cast<size_t>(c / ytile) * y_frames + f) * n_station + s) * ytile +
            (c % ytile);
-}
-
-/// Channels per spectra tile for n_station inputs: 8 while 8 accumulators of
-/// 2N (rounded to 16) TMEM columns fit in 512 columns (N <= 32), else 4.
-inline int ytile_for(int n_station) {
-    const int n_mma = std::max(16, (2 * n_station + 15) / 16 * 16);
-    return 8 * n_mma <= 512 ? 8 : 4;
 }
 
 /// Arguments of one F-engine launch: `frames` x `n_station` real FFTs.
@@ -112,10 +105,17 @@ corr_status xengine_plain_launch(const XengineArgs &a, int num_sms, cudaStream_t
 corr_status scale_launch(float2 *acc, size_t n, float s, cudaStream_t stream);
 corr_status watchdog_selftest_launch(int *err, long long budget_cycles, cudaStream_t stream);
 corr_status stamp_launch(unsigned long long *slot, cudaStream_t stream);
+/// Deterministic pseudo-random int8 samples (roughly Gaussian, sigma ~ 24) for
+/// the autotuner's timing passes.
+corr_status synth_fill_launch(int8_t *x, size_t n, uint32_t seed, cudaStream_t stream);
 
 // xengine_tc.cu
-size_t xengine_tc_workspace_bytes(int n_station, int n_freq);
-corr_status xengine_tc_launch(const XengineArgs &a, bool split, int num_sms,
+/// Is (ct channels per tile, kt frames per stage) a feasible tensor X-engine
+/// tile for n_station inputs (TMEM columns, shared memory)?
+bool xengine_tc_shape_ok(int n_station, bool split, int ct, int kt);
+/// The widest feasible tile with 16-frame stages (*ct = 0: none).
+void xengine_tc_default_shape(int n_station, bool split, int *ct, int *kt);
+corr_status xengine_tc_launch(const XengineArgs &a, bool split, int ct, int kt, int num_sms,
                               cudaStream_t stream);
 
 /// An FX plan: everything one device needs to turn int8 frames into added
@@ -126,7 +126,9 @@ struct FxPlan {
     int n_freq = 0;
     int n_baseline = 0;
     int max_frames = 0;   // frames per F/X pass (spectra buffer depth)
-    int ytile = 8;        // channels per spectra tile (ytile_for(n_station))
+    int ytile = 0;        // channels per spectra tile (n_freq: contiguous rows)
+    int xct = 0;          // tensor X-engine: channels per tile
+    int xkt = 0;          // tensor X-engine: frames per stage
     int xmode = CORR_X_PLAIN_FP32;
     int num_sms = 0;
     float2 *d_y = nullptr;
@@ -137,6 +139,8 @@ struct FxPlan {
 corr_status fxplan_create(int device, int n_station, int n_freq, int max_frames, int xmode,
                           FxPlan **out);
 void fxplan_destroy(FxPlan *p);
+corr_status fxplan_set_tiles(FxPlan *p, int ytile, int xct, int xkt);
+corr_status fxplan_autotune(FxPlan *p, cudaStream_t stream, corrx_tiles *out);
 
 /// F then X over `frames` frames, in passes of at most max_frames.
 corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_stride,

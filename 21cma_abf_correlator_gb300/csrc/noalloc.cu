@@ -151,19 +151,21 @@ extern "C" corr_status corrx_accumulate_noalloc(int32_t n_station, int32_t n_fre
     fa.frames = frames;
     fa.y = d.spectra;
     fa.y_frames = frames;
-    fa.ytile = ytile_for(n_station);
+    fa.ytile = n_freq;
     fa.err = nullptr;
     if ((st = fengine_launch(n_freq, tw, fa, d.num_sms, s)) != CORR_OK) return st;
 
     XengineArgs xa{};
     xa.y = d.spectra;
     xa.y_frames = frames;
-    xa.ytile = ytile_for(n_station);
+    xa.ytile = n_freq;
     xa.n_station = n_station;
     xa.n_freq = n_freq;
     xa.frames = frames;
     xa.acc = static_cast<float2 *>(d_acc);
     xa.err = nullptr;
     if (xmode == CORR_X_PLAIN_FP32) return xengine_plain_launch(xa, d.num_sms, s);
-    return xengine_tc_launch(xa, xmode == CORR_X_TC_FP16_SPLIT, d.num_sms, s);
+    int ct = 0, kt = 0;
+    xengine_tc_default_shape(n_station, xmode == CORR_X_TC_FP16_SPLIT, &ct, &kt);
+    return xengine_tc_launch(xa, xmode == CORR_X_TC_FP16_SPLIT, ct, kt, d.num_sms, s);
 }

@@ -65,13 +65,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 }
 
 // Wait for phase `parity` of `bar` to complete, for at most kWaitBudgetCycles.
-// On timeout writes `code` into *err and returns false.
+// On timeout writes `code` into *err and returns false. With `abort` given, also
+// returns false (recording nothing) as soon as *abort becomes non-zero: another
+// role of the CTA already gave up and recorded why.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int *err,
-                                                  int code) {
+                                                  int code,
+                                                  const volatile int *abort = nullptr) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     while (true) {
         if (mbar_try_wait(bar, parity)) return true;
+        if (abort != nullptr && *abort != 0) return false;
         if (clock64() - t0 > kWaitBudgetCycles) {
             if (err != nullptr) atomicExch(err, code);
             return false;

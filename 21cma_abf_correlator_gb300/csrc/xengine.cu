@@ -57,11 +57,15 @@ __global__ void __launch_bounds__(1024, 1)
     const int chunks = stage_elems / 2;   // 16-byte pieces per stage
     const int n_stages = (frames + kXfs - 1) / kXfs;
 
+    // Every thread copies the same two channels (blockDim is a multiple of 16):
+    // piece `part` of each (frame, station) row of the stage.
+    const int part = threadIdx.x & 15;
+    const int cq = c0 + part * 2;
+    const float2 *ybase = y + y_index(cq, 0, 0, n_station, y_frames, ytile);
     auto load_stage = [&](int s) {
         float2 *dst = xs + (s % kXstages) * stage_elems;
         const int f0 = s * kXfs;
         for (int q = threadIdx.x; q < chunks; q += nthreads) {
-            const int part = q & 15;                 // 16 pieces of 16 B per row
             const int row = q >> 4;                  // frame*npad + station
             const int fi = row / npad;
             const int st = row - fi * npad;
@@ -69,7 +73,7 @@ __global__ void __launch_bounds__(1024, 1)
             const bool ok = (st < n_station) && (f < frames);
             // two channels per 16-byte piece, inside one channel tile
             const float2 *src =
-                ok ? y + y_index(c0 + part * 2, f, st, n_station, y_frames, ytile) : y;
+                ok ? ybase + (static_cast<size_t>(f) * n_station + st) * ytile : y;
             cp_async16(dst + row * kXch + part * 2, src, ok ? 16u : 0u);
         }
     };
@@ -208,6 +212,37 @@ corr_status scale_launch(float2 *acc, size_t n, float s, cudaStream_t stream) {
     if (blocks > 4096) blocks = 4096;
     scale_kernel<<<static_cast<unsigned>(blocks), 256, 0, stream>>>(acc, n, s);
     return cuda_check(cudaGetLastError(), "scale_kernel launch");
+}
+
+// MurmurHash3's 32-bit finaliser (a published integer mixing function).
+__device__ __forceinline__ uint32_t mix32(uint32_t h) {
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    return h;
+}
+
+// Sum of four uniform bytes, centred and scaled: close to N(0, 24^2), in int8.
+__global__ void synth_fill_kernel(int8_t *x, size_t n, uint32_t seed) {
+    const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+    for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += stride) {
+        const uint32_t h = mix32(static_cast<uint32_t>(i) ^ mix32(static_cast<uint32_t>(i >> 32) + seed));
+        const int sum = static_cast<int>((h & 0xff) + ((h >> 8) & 0xff) + ((h >> 16) & 0xff) +
+                                         (h >> 24)) - 510;
+        const int v = __float2int_rn(static_cast<float>(sum) * 0.1624f);
+        x[i] = static_cast<int8_t>(max(-127, min(127, v)));
+    }
+}
+
+corr_status synth_fill_launch(int8_t *x, size_t n, uint32_t seed, cudaStream_t stream) {
+    if (n == 0) return CORR_OK;
+    size_t blocks = (n + 255) / 256;
+    if (blocks > 16384) blocks = 16384;
+    synth_fill_kernel<<<static_cast<unsigned>(blocks), 256, 0, stream>>>(x, n, seed);
+    return cuda_check(cudaGetLastError(), "synth_fill_kernel launch");
 }
 
 corr_status stamp_launch(unsigned long long *slot, cudaStream_t stream) {

@@ -1,7 +1,7 @@
-// xengine_tc.cu -- tensor-core X-engine: tcgen05 MMA, FP16 spectra, FP32 in TMEM.
+// xengine_tc.cu -- tensor-core X-engine: tcgen05 MMA, FP16 operands, FP32 in TMEM.
 //
 // The same sum as the plain X-engine (reference corr_kernel,
-// corr-cuda/src/kernels.cu:194-265), recast as one small real GEMM per channel.
+// corr-cuda/src/kernels.cu:194-265), recast as small real GEMMs per channel.
 // For channel c let D be the frames x 2N real matrix whose columns are
 // (Re Y_0, Im Y_0, Re Y_1, Im Y_1, ...). Then S = D^T D holds everything:
 //     Re V[j,k] = S[2j][2k] + S[2j+1][2k+1]
@@ -10,10 +10,9 @@
 // in tensor memory (TMEM), accumulated over the whole launch.
 //
 // Precision forms:
-//   FP16       : D rounded once to FP16 (11-bit significand); one MMA per K step.
-//   FP16 split : D = Dh + Dl, Dh = fp16(D), Dl = fp16(D - Dh) (about 22 bits).
-//                S ~ Dh^T Dh + Dh^T Dl + Dl^T Dh, the Dl^T Dl term dropped: three
-//                MMAs per K step into the same accumulator.
+//   FP16       : D rounded once to FP16 (11-bit significand).
+//   FP16 split : D = Dh + Dl, Dh = fp16(D), Dl = fp16(D - Dh) (about 22 bits);
+//                S ~ H + P + P^T with H = Dh^T Dh and P = Dl^T Dh (Dl^T Dl dropped).
 // Scale: spectra of int8 frames satisfy |Y| <= 128*L, so multiplying by the
 // power of two 2^-(log2 L - 8) keeps every value below 2^15 (< FP16 max) in
 // every channel for every input; being a power of two it is undone exactly.
@@ -21,23 +20,41 @@
 // data, so the scaled values sit in FP16's normal range and no per-channel
 // adaptive scale is needed.
 //
+// Operand regions. Per K step each region gets exactly one MMA: M = 128 rows of
+// A read from the region's start, N = nb rows of B from the same start.
+// R = 2N rounded up to 8 (the rows of one channel's D):
+//   split, N <= 32 ("stacked"): rows [0,2N) Dh, [R,R+2N) Dl; nb = 2N (to 16):
+//       TMEM lanes [0,2N) x cols [0,2N) = H, lanes [R,R+2N) x cols [0,2N) = P.
+//   split, N > 32 ("wide"):  same rows; nb = R+2N (to 16), so B carries Dl and
+//       lanes [0,2N) hold H in cols [0,2N) and T = Dh^T Dl = P^T in [R,R+2N).
+//   fp16, N <= 32 ("paired"): two channels per region, rows [0,2N) and [R,R+2N);
+//       nb = R+2N (to 16): the two diagonal blocks are the two channels' S.
+//   fp16, N > 32: one channel per region, rows [0,2N), nb = 2N (to 16).
+// The cross term: with Q[j][k] formed from rows 2j, 2j+1 of P exactly as V from
+// S, P + P^T adds Q[j][k] + conj(Q[k][j]) to V[j][k] (the same holds with T in
+// place of P), so the epilogue stages Q and folds it in as it adds V to the row.
+// An MMA with M = 128 reads 4 KB of A whatever the form; stacking the split
+// operands (pairing channels) makes that read serve three (two) products
+// instead of one, which keeps the tensor cores' shared-memory reads below the
+// stage's DRAM time.
+//
 // Warp-specialised persistent CTAs, one per SM (TMEM), CT channels per tile:
-//   control warp (lane 0): one TMA bulk copy per stage -- KT = 16 frames x N
-//     stations of one CT-channel spectra tile, a contiguous block in the
-//     channel-tiled layout -- into a ring as deep as shared memory allows (up to
-//     6 stages); tcgen05.mma issue (M=128, N=2N rounded to 16, K=16) once a
-//     stage's operands are ready; commits.
-//   8 worker warps convert a landed stage (scale, round, split) into the
-//     K-major no-swizzle UMMA operand layout (8-row x 16-byte core matrices,
-//     2-deep ring); after a tile's last stage, read the accumulators
-//     (tcgen05.ld), pair rows 2j/2j+1 with one shuffle to form V, and add V into
-//     the row with fire-and-forget reductions.
-// The roles meet only at mbarriers (stage full/empty, accumulator full/empty),
-// all waited on with clock-bounded waits, so a stuck party makes the others
-// time out and report instead of hanging.
+//   warp 0 (lane 0): TMA tensor loads -- one 4-D box {CT channels, N stations,
+//     KT frames, 1 tile} of the spectra per stage, into a ring as deep as shared
+//     memory allows -- and the MMAs of a stage once its operands are written.
+//   warps 1-8 (converters): scale, round and split a landed stage into the
+//     K-major no-swizzle operand layout (8-row x 16-byte core matrices).
+//   warps 9-12 (epilogue, one per TMEM lane quarter): after a tile's last MMA,
+//     read the accumulators (tcgen05.ld), pair rows 2j/2j+1 with one shuffle,
+//     stage V (and Q), release TMEM, then add V into the row in global memory
+//     with 16-byte read-modify-writes (one owner per channel tile and launch).
+// The roles meet only at mbarriers, all waited on with clock-bounded waits, so
+// a stuck party makes the others time out and report instead of hanging.
 
 #include <algorithm>
+#include <mutex>
 
+#include <cuda.h>
 #include <cuda_fp16.h>
 
 #include "engine.h"
@@ -46,81 +63,121 @@
 namespace corrgb {
 namespace {
 
-constexpr int kWorkers = 256;                // 8 worker warps
-constexpr int kThreads = 32 + kWorkers;      // + control warp
-constexpr int kKT = 16;                      // frames per stage = one MMA K step
-constexpr int kMaxLoadStages = 6;            // fp32 ring depth (TMA), as smem allows
-constexpr int kOpStages = 2;                 // operand ring depth
-constexpr int kSBO = (kKT / 8) * 128;        // bytes per 8-row group (all K of a stage)
-constexpr int kLBO = 128;                    // bytes between K-adjacent core matrices
+constexpr int kConverters = 256;                 // warps 1-8
+constexpr int kEpilogue = 128;                   // warps 9-12
+constexpr int kThreads = 32 + kConverters + kEpilogue;
+constexpr int kMaxLoadStages = 6;
+constexpr int kMaxOpStages = 3;
+constexpr int kMaxItems = 4;                     // conversion items per converter thread
+constexpr int kLBO = 128;                        // bytes between K-adjacent core matrices
+
+enum TcForm : int { kSplitStacked = 0, kSplitWide = 1, kFp16Paired = 2, kFp16Wide = 3 };
 
 struct TcGeom {
     int n_station;
-    int lo_row;        // first Dl row (2N rounded up to 8); split form only
-    int rows_valid;    // rows written per channel
-    int n_mma;         // 2N rounded up to a multiple of 16 (MMA N, TMEM columns)
-    int ct;            // channels per tile
-    int tmem_cols;     // allocated columns (power of two >= 32)
-    int chan_stride;   // operand bytes per channel region (multiple of 128, one 128 B pad)
-    int op_stage;      // operand bytes per stage (incl. bank skew and the last A's reach)
-    int ld_stage;      // fp32 bytes per stage = KT * N * CT * 8
-    int n_ld;          // fp32 ring depth (2..kMaxLoadStages)
-    int vs_bytes;      // epilogue staging of V
-    int smem;
+    int form;
     bool split;
+    int ct;            // channels per tile
+    int kt;            // frames per stage (16 or 32)
+    int R;             // rows of one channel's D (2N rounded up to 8)
+    int nb;            // MMA N
+    int regions;       // operand regions per stage
+    int sbo;           // bytes between 8-row groups = (kt/8) * 128
+    int region_stride; // bytes between regions (multiple of 128, one 128-byte pad)
+    int tmem_cols;
+    int op_stage;      // operand bytes per stage
+    int ld_stage;      // fp32 bytes per stage = kt * N * ct * 8
+    int n_ld;
+    int n_op;
+    int vs_bytes;      // staged V: n_baseline x ct float2
+    int qs_bytes;      // staged Q: N*N x ct float2 (split forms)
+    int smem;
+    int items;         // conversion items per stage = ct * N * kt/8
+    bool ok;
 };
 
-TcGeom make_geom(int n_station, bool split) {
+int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+// 16-byte bank skew of region r: the eight 16-byte stores of a quarter warp
+// (eight channels, one station) land in eight distinct slots of a bank line.
+__host__ __device__ inline int region_skew(int r) {
+    return ((r & 1) | ((r & 2) << 1) | ((r & 4) >> 1)) * 16;
+}
+
+TcGeom make_geom(int n_station, bool split, int ct, int kt) {
     TcGeom g{};
+    g.ok = false;
     g.n_station = n_station;
     g.split = split;
-    g.lo_row = (2 * n_station + 7) / 8 * 8;
-    g.rows_valid = split ? g.lo_row + 2 * n_station : 2 * n_station;
-    g.n_mma = std::max(16, (2 * n_station + 15) / 16 * 16);
-    int ct = 8;
-    while (ct > 2 && ct * g.n_mma > 512) ct /= 2;
     g.ct = ct;
+    g.kt = kt;
+    const int N = n_station;
+    if (N < 1 || N > 64 || (kt != 16 && kt != 32) || ct < 2 || ct > 8 || (ct & (ct - 1)))
+        return g;
+    g.R = round_up(2 * N, 8);
+    int rows_valid;
+    if (split) {
+        g.form = (g.R + 2 * N <= 128) ? kSplitStacked : kSplitWide;
+        g.nb = g.form == kSplitStacked ? std::max(16, round_up(2 * N, 16))
+                                       : round_up(g.R + 2 * N, 16);
+        g.regions = ct;
+        rows_valid = g.R + 2 * N;
+    } else {
+        g.form = (g.R + 2 * N <= 128) ? kFp16Paired : kFp16Wide;
+        g.nb = g.form == kFp16Paired ? round_up(g.R + 2 * N, 16)
+                                     : std::max(16, round_up(2 * N, 16));
+        g.regions = g.form == kFp16Paired ? ct / 2 : ct;
+        rows_valid = g.form == kFp16Paired ? g.R + 2 * N : 2 * N;
+    }
+    if (g.nb > 256) return g;
+    // highest TMEM column any epilogue read touches (reads are 16 columns wide)
+    int max_col = g.regions * g.nb;
+    const int chunk = round_up(2 * N, 16);
+    if (g.form == kSplitWide) max_col = std::max(max_col, (ct - 1) * g.nb + g.R + chunk);
+    if (g.form == kFp16Paired)
+        max_col = std::max(max_col, (g.regions - 1) * g.nb + g.R + chunk);
     int cols = 32;
-    while (cols < ct * g.n_mma) cols *= 2;
+    while (cols < max_col) cols *= 2;
+    if (cols > 512) return g;
     g.tmem_cols = cols;
-    const int groups = (g.rows_valid + 7) / 8;
-    // The 128-byte pad keeps a region plus its bank skew (<= 112 B) clear of the
-    // next channel's region, whatever the skews of the two.
-    g.chan_stride = groups * kSBO + 128;
-    // A reads 128 rows from Dh (and from Dl in the split form): the last
-    // channel's reach past its own rows, plus the largest bank skew (7*16 B).
-    const int reach = ((split ? g.lo_row : 0) + 128 + 7) / 8 * kSBO;
-    const int slack = std::max(0, reach - g.chan_stride) + 7 * 16 + 128;
-    g.op_stage = (g.ct * g.chan_stride + slack + 127) / 128 * 128;
-    g.ld_stage = kKT * n_station * g.ct * 8;
-    g.vs_bytes = n_station * (n_station + 1) / 2 * g.ct * 8;
-    // As many TMA stages in flight as shared memory holds: the loads are rows of
-    // 8*CT bytes scattered n_freq*8 bytes apart, so latency, not bandwidth, sets
-    // how many must be outstanding.
-    const int fixed = kOpStages * g.op_stage + g.vs_bytes + 128;
-    g.n_ld = std::max(2, std::min(kMaxLoadStages, (227 * 1024 - 1024 - fixed) / g.ld_stage));
-    g.smem = g.n_ld * g.ld_stage + fixed;
+    g.sbo = (kt / 8) * 128;
+    const int groups = (rows_valid + 7) / 8;
+    g.region_stride = groups * g.sbo + 128;
+    // A reads 128 rows (16 groups), B nb rows, from the last region's start,
+    // plus its skew.
+    const int reach = std::max(16, g.nb / 8) * g.sbo;
+    const int slack = std::max(0, reach - g.region_stride) + 7 * 16 + 128;
+    g.op_stage = round_up(g.regions * g.region_stride + slack, 128);
+    g.ld_stage = kt * N * ct * 8;
+    g.items = ct * N * (kt / 8);
+    if (g.items > kMaxItems * kConverters) return g;
+    const int n_baseline = N * (N + 1) / 2;
+    g.vs_bytes = round_up(n_baseline * ct * 8, 128);
+    g.qs_bytes = split ? round_up(N * N * ct * 8, 128) : 0;
+    const int jk_bytes = round_up(n_baseline * 2, 128);
+    const int budget = 227 * 1024 - 1024;
+    const int fixed = g.vs_bytes + g.qs_bytes + jk_bytes + 128;
+    g.n_op = 2;
+    if (fixed + g.n_op * g.op_stage + 2 * g.ld_stage > budget) return g;
+    // a third operand stage when it still leaves a four-deep load ring
+    if (fixed + 3 * g.op_stage + 4 * g.ld_stage <= budget) g.n_op = 3;
+    g.n_ld = std::min(kMaxLoadStages, (budget - fixed - g.n_op * g.op_stage) / g.ld_stage);
+    g.smem = g.n_ld * g.ld_stage + g.n_op * g.op_stage + fixed;
     // Two CTAs on one SM would both need more than half of TMEM and the second
     // would stall in tcgen05.alloc for the first's whole (persistent) life:
     // claim more than half of shared memory so the scheduler never pairs them.
     if (g.tmem_cols > 256) g.smem = std::max(g.smem, 120 * 1024);
+    g.ok = true;
     return g;
-}
-
-// 16-byte bank skew of channel c's operand region: with lanes ordered (channel,
-// station), the eight 16-byte stores of a quarter warp land in eight distinct
-// slots of a 128-byte bank line for CT = 8 (one station) and CT = 4 (two).
-__host__ __device__ inline int chan_skew(int c) {
-    return ((c & 1) | ((c & 2) << 1) | ((c & 4) >> 1)) * 16;
 }
 
 // --- tcgen05 / TMA wrappers -------------------------------------------------
 
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, int sbo) {
     // K-major, no swizzle: start>>4 | LBO>>4 << 16 | SBO>>4 << 32 | descriptor version 1 << 46
     return static_cast<uint64_t>((addr >> 4) & 0x3FFFu) |
            (static_cast<uint64_t>((kLBO >> 4) & 0x3FFF) << 16) |
-           (static_cast<uint64_t>((kSBO >> 4) & 0x3FFF) << 32) | (1ull << 46);
+           (static_cast<uint64_t>((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
 }
 
 __device__ __forceinline__ uint32_t instr_desc_f16_f32(int m, int n) {
@@ -169,9 +226,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// Byte offset of (row r, frame group kq of 8) inside one channel's operand region.
-__device__ __forceinline__ int core_off(int r, int kq) {
-    return (r >> 3) * kSBO + kq * kLBO + (r & 7) * 16;
+// 4-D TMA tile load global -> shared, completing on `bar`.
+__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, int x, int y, int z,
+                                            int w, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(w),
+        "r"(smem_addr(bar))
+        : "memory");
 }
 
 __device__ __forceinline__ uint32_t half2_bits(__half2 h) {
@@ -179,8 +242,7 @@ __device__ __forceinline__ uint32_t half2_bits(__half2 h) {
 }
 
 struct TcParams {
-    const float2 *y;
-    int y_frames;
+    int ytile;
     int n_station;
     int n_freq;
     int frames;
@@ -192,22 +254,23 @@ struct TcParams {
 };
 
 struct TcBars {
-    uint64_t load_full[kMaxLoadStages];   // a stage's bulk copy landed (tx-count)
-    uint64_t op_full[kOpStages];       // workers wrote a stage's operands (256 arrivals)
-    uint64_t op_empty[kOpStages];      // MMAs reading an operand buffer finished (commit)
-    uint64_t acc_full;                 // a tile's MMAs finished (commit)
-    uint64_t acc_empty;                // workers finished reading the accumulators (256)
-    uint64_t epi;                      // worker-only sync inside the epilogue (256)
-    uint64_t fin;                      // abort path: everything this CTA issued landed
+    uint64_t load_full[kMaxLoadStages];  // a stage's TMA load landed (tx-count)
+    uint64_t op_full[kMaxOpStages];      // converters wrote a stage's operands (256 arrivals)
+    uint64_t op_empty[kMaxOpStages];     // MMAs reading an operand buffer finished (commit)
+    uint64_t acc_full;                   // a tile's MMAs finished (commit)
+    uint64_t acc_empty;                  // epilogue read the accumulators (128 arrivals)
+    uint64_t epi;                        // epilogue-only sync (128 arrivals, twice per tile)
+    uint64_t fin;                        // abort path: every MMA this CTA issued finished
 };
 
-__global__ void __launch_bounds__(kThreads, 1) xengine_tc_kernel(TcParams p) {
+__global__ void __launch_bounds__(kThreads, 1)
+    xengine_tc_kernel(const __grid_constant__ CUtensorMap ymap, TcParams p) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char *smem = smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127);
     __shared__ TcBars bars;
     __shared__ uint32_t s_tmem_base;
     __shared__ int s_abort;
-    __shared__ uint32_t s_ld_issued;   // bulk copies issued (abort drain)
+    __shared__ uint32_t s_ld_issued;   // TMA loads issued (abort drain)
 
     const TcGeom &g = p.g;
     const int tid = threadIdx.x;
@@ -217,24 +280,38 @@ __global__ void __launch_bounds__(kThreads, 1) xengine_tc_kernel(TcParams p) {
     const int n_tiles = p.n_freq / g.ct;
     const int my_tiles = (n_tiles - static_cast<int>(blockIdx.x) + static_cast<int>(gridDim.x) - 1) /
                          static_cast<int>(gridDim.x);
-    const int n_stages = (p.frames + kKT - 1) / kKT;
+    const int n_stages = (p.frames + g.kt - 1) / g.kt;
     const int total = my_tiles * n_stages;
-    float *ld_ring = reinterpret_cast<float *>(smem);
-    const int n_ld = g.n_ld;
-    unsigned char *op_ring = smem + n_ld * g.ld_stage;
-    float2 *Vs = reinterpret_cast<float2 *>(op_ring + kOpStages * g.op_stage);
+    const int n_baseline = N * (N + 1) / 2;
+    unsigned char *ld_ring = smem;
+    unsigned char *op_ring = smem + g.n_ld * g.ld_stage;
+    float2 *Vs = reinterpret_cast<float2 *>(op_ring + g.n_op * g.op_stage);
+    float2 *Qs = reinterpret_cast<float2 *>(reinterpret_cast<unsigned char *>(Vs) + g.vs_bytes);
+    uint16_t *jk = reinterpret_cast<uint16_t *>(reinterpret_cast<unsigned char *>(Qs) + g.qs_bytes);
 
-    for (int i = tid; i < kOpStages * g.op_stage / 16; i += kThreads)
+    // Operand rows no conversion writes (a region's padding rows, the reach of
+    // the last region's A) must hold finite values: zero them once, and make
+    // the zeros visible to the tensor cores' (async-proxy) reads.
+    for (int i = tid; i < g.n_op * g.op_stage / 16; i += kThreads)
         reinterpret_cast<uint4 *>(op_ring)[i] = make_uint4(0, 0, 0, 0);
+    fence_proxy_async_smem();
+    for (int b = tid; b < n_baseline; b += kThreads) {
+        int j = 0, rem = b;
+        while (rem >= N - j) {
+            rem -= N - j;
+            ++j;
+        }
+        jk[b] = static_cast<uint16_t>((j << 8) | (j + rem));
+    }
     if (tid == 0) {
-        for (int s = 0; s < n_ld; ++s) mbar_init(&bars.load_full[s], 1);
-        for (int s = 0; s < kOpStages; ++s) {
-            mbar_init(&bars.op_full[s], kWorkers);
+        for (int s = 0; s < g.n_ld; ++s) mbar_init(&bars.load_full[s], 1);
+        for (int s = 0; s < g.n_op; ++s) {
+            mbar_init(&bars.op_full[s], kConverters);
             mbar_init(&bars.op_empty[s], 1);
         }
         mbar_init(&bars.acc_full, 1);
-        mbar_init(&bars.acc_empty, kWorkers);
-        mbar_init(&bars.epi, kWorkers);
+        mbar_init(&bars.acc_empty, kEpilogue);
+        mbar_init(&bars.epi, kEpilogue);
         mbar_init(&bars.fin, 1);
         s_abort = 0;
         s_ld_issued = 0;
@@ -251,130 +328,118 @@ __global__ void __launch_bounds__(kThreads, 1) xengine_tc_kernel(TcParams p) {
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = s_tmem_base;
+    const volatile int *abort_flag = &s_abort;
 
     auto tile_c0 = [&](int tl) {
         return (static_cast<int>(blockIdx.x) + tl * static_cast<int>(gridDim.x)) * g.ct;
     };
 
     if (warp == 0) {
-        // ------------------------------ control ------------------------------
+        // ------------------------- loads + MMAs -------------------------
         if (lane == 0) {
-            // Stage gs = frames [f0, f0+KT) of this CTA's tile: one contiguous
-            // block of the spectra; frames past the buffer are left stale and
-            // zeroed by the conversion (f >= frames).
-            const size_t tile_elems = static_cast<size_t>(p.y_frames) * N * g.ct;
+            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&ymap))
+                         : "memory");
             auto issue = [&](int gs) {
                 const int tl = gs / n_stages;
                 const int st = gs - tl * n_stages;
-                const int slot = gs % n_ld;
-                const int f0 = st * kKT;
-                const int nfr = min(kKT, p.y_frames - f0);
-                const uint32_t bytes = static_cast<uint32_t>(nfr) * N * g.ct * 8;
-                const int tile = tile_c0(tl) / g.ct;
-                const float2 *src = p.y + tile * tile_elems + static_cast<size_t>(f0) * N * g.ct;
-                mbar_arrive_expect_tx(&bars.load_full[slot], bytes);
-                bulk_copy_g2s(ld_ring + slot * (g.ld_stage / 4), src, bytes, &bars.load_full[slot]);
+                const int slot = gs % g.n_ld;
+                const int c0 = tile_c0(tl);
+                mbar_arrive_expect_tx(&bars.load_full[slot], static_cast<uint32_t>(g.ld_stage));
+                // frames past the buffer's end arrive as zeros; frames in
+                // [frames, y_frames) are stale and the converters zero them
+                tma_load_4d(ld_ring + slot * g.ld_stage, &ymap, c0 & (p.ytile - 1), 0, st * g.kt,
+                            c0 / p.ytile, &bars.load_full[slot]);
                 ++s_ld_issued;
             };
-            for (int gs = 0; gs < n_ld && gs < total; ++gs) issue(gs);
-            const uint32_t idesc = instr_desc_f16_f32(128, g.n_mma);
-            uint32_t ph_full = 0, ph_acc_empty = 0;
-            for (int gs = 0; gs < total && !s_abort; ++gs) {
+            for (int gs = 0; gs < g.n_ld && gs < total; ++gs) issue(gs);
+            const uint32_t idesc = instr_desc_f16_f32(128, g.nb);
+            const int ksteps = g.kt / 16;
+            for (int gs = 0; gs < total && *abort_flag == 0; ++gs) {
                 const int tl = gs / n_stages;
                 const int st = gs - tl * n_stages;
-                const int ob = gs & 1;
+                const int ob = gs % g.n_op;
                 if (st == 0 && tl > 0) {
                     // the previous tile's accumulators must be read before overwrite
-                    if (!mbar_wait_bounded(&bars.acc_empty, ph_acc_empty, p.err,
-                                           kErrXengineMmaTimeout)) {
+                    if (!mbar_wait_bounded(&bars.acc_empty, static_cast<uint32_t>(tl - 1) & 1u,
+                                           p.err, kErrXengineMmaTimeout, abort_flag)) {
                         s_abort = 1;
                         break;
                     }
-                    ph_acc_empty ^= 1u;
                 }
-                if (!mbar_wait_bounded(&bars.op_full[ob], (ph_full >> ob) & 1u, p.err,
-                                       kErrXengineMmaTimeout)) {
+                if (!mbar_wait_bounded(&bars.op_full[ob], static_cast<uint32_t>(gs / g.n_op) & 1u,
+                                       p.err, kErrXengineMmaTimeout, abort_flag)) {
                     s_abort = 1;
                     break;
                 }
-                ph_full ^= 1u << ob;
                 tc_fence_after();
                 const uint32_t base = smem_addr(op_ring + ob * g.op_stage);
-                const uint32_t acc_flag = st > 0 ? 1u : 0u;
-                for (int c = 0; c < g.ct; ++c) {
-                    const uint32_t chb = base + c * g.chan_stride + chan_skew(c);
-                    const uint32_t d = tmem + static_cast<uint32_t>(c * g.n_mma);
-                    const uint64_t hdesc = smem_desc(chb);
-                    umma_f16(d, hdesc, hdesc, idesc, acc_flag);
-                    if (g.split) {
-                        const uint64_t ldesc = smem_desc(chb + (g.lo_row / 8) * kSBO);
-                        umma_f16(d, hdesc, ldesc, idesc, 1u);
-                        umma_f16(d, ldesc, hdesc, idesc, 1u);
+                for (int r = 0; r < g.regions; ++r) {
+                    const uint32_t rb = base + r * g.region_stride + region_skew(r);
+                    const uint32_t d = tmem + static_cast<uint32_t>(r * g.nb);
+                    for (int ks = 0; ks < ksteps; ++ks) {
+                        const uint64_t desc = smem_desc(rb + ks * 2 * kLBO, g.sbo);
+                        umma_f16(d, desc, desc, idesc, (st > 0 || ks > 0) ? 1u : 0u);
                     }
                 }
                 umma_commit(&bars.op_empty[ob]);
                 if (st == n_stages - 1) umma_commit(&bars.acc_full);
-                // op_full for this stage means every worker has read its fp32
-                // slot: refill the slot n_ld stages ahead.
-                if (gs + n_ld < total) {
-                    fence_proxy_async_smem();
-                    issue(gs + n_ld);
-                }
+                // op_full for this stage means every converter has read its
+                // fp32 slot: refill the slot n_ld stages ahead.
+                if (gs + g.n_ld < total) issue(gs + g.n_ld);
             }
         }
-    } else {
-        // ------------------------------ workers ------------------------------
+    } else if (warp <= kConverters / 32) {
+        // --------------------------- converters ---------------------------
         const int wt = tid - 32;
-        const int items = g.ct * N * (kKT / 8);
-        const int quad = warp & 3;                 // TMEM lanes this warp may read
-        const int half = (warp - 1) >> 2;          // column-chunk parity
-        const int nchunks = g.n_mma / 16;
-        const int n_baseline = N * (N + 1) / 2;
-        uint32_t ph_load = 0, ph_empty = 0, ph_acc = 0, ph_epi = 0;
-        // Conversion: this thread's items (channel c, station s, 8-frame group kq)
-        // are also the same every stage; keep their fp32 read offsets, operand
-        // write offsets and first frame.
-        constexpr int kMaxItems = (8 * 44 * (kKT / 8) + kWorkers - 1) / kWorkers;
+        // This thread's items (channel c, station s, 8-frame group kq) are the
+        // same every stage: keep their fp32 offsets, operand offsets, frames.
         int n_item = 0;
         uint32_t it_ld[kMaxItems], it_op[kMaxItems];
         int it_f[kMaxItems];
+        const int lo_off = (g.R / 8) * g.sbo;   // Dl rows start at row R
 #pragma unroll
         for (int i = 0; i < kMaxItems; ++i) {
-            const int q = wt + i * kWorkers;
-            if (q < items) {
+            it_ld[i] = 0;
+            it_op[i] = 0;
+            it_f[i] = 0;
+            const int q = wt + i * kConverters;
+            if (q < g.items) {
                 const int c = q % g.ct;
                 const int rest = q / g.ct;
                 const int s = rest % N;
                 const int kq = rest / N;
+                int region = c, row = 2 * s;
+                if (g.form == kFp16Paired) {
+                    region = c >> 1;
+                    row += (c & 1) * g.R;
+                }
                 it_ld[i] = static_cast<uint32_t>((kq * 8 * N + s) * g.ct + c);
-                it_op[i] = static_cast<uint32_t>(c * g.chan_stride + chan_skew(c) + core_off(2 * s, kq));
+                it_op[i] = static_cast<uint32_t>(region * g.region_stride + region_skew(region) +
+                                                 (row >> 3) * g.sbo + kq * kLBO + (row & 7) * 16);
                 it_f[i] = kq * 8;
                 n_item = i + 1;
             }
         }
-        const int row_step = N * g.ct;               // float2 between consecutive frames
-        const int lo_off = (g.lo_row / 8) * kSBO;    // Dl rows start here (row 2s -> lo_row + 2s)
+        const int row_step = N * g.ct;   // float2 between consecutive frames of a slot
         for (int gs = 0; gs < total; ++gs) {
             const int tl = gs / n_stages;
             const int st = gs - tl * n_stages;
-            const int lb = gs % n_ld;
-            const int ob = gs & 1;
-            bool ok = mbar_wait_bounded(&bars.load_full[lb], (ph_load >> lb) & 1u, p.err,
-                                        kErrXengineMmaTimeout);
-            ph_load ^= 1u << lb;
-            if (ok && gs >= kOpStages) {
-                ok = mbar_wait_bounded(&bars.op_empty[ob], (ph_empty >> ob) & 1u, p.err,
-                                       kErrXengineMmaTimeout);
-                ph_empty ^= 1u << ob;
-            }
+            const int lb = gs % g.n_ld;
+            const int ob = gs % g.n_op;
+            bool ok = mbar_wait_bounded(&bars.load_full[lb], static_cast<uint32_t>(gs / g.n_ld) & 1u,
+                                        p.err, kErrXengineMmaTimeout, abort_flag);
+            if (ok && gs >= g.n_op)
+                ok = mbar_wait_bounded(&bars.op_empty[ob],
+                                       static_cast<uint32_t>(gs / g.n_op - 1) & 1u, p.err,
+                                       kErrXengineMmaTimeout, abort_flag);
             if (!ok) {
                 s_abort = 1;
                 break;
             }
             // fp32 slot: [frame][station][CT channels]
-            const float2 *ld = reinterpret_cast<const float2 *>(ld_ring + lb * (g.ld_stage / 4));
+            const float2 *ld = reinterpret_cast<const float2 *>(ld_ring + lb * g.ld_stage);
             unsigned char *op = op_ring + ob * g.op_stage;
-            const int f0 = st * kKT;
+            const int f0 = st * g.kt;
 #pragma unroll
             for (int it = 0; it < kMaxItems; ++it) {
                 if (it >= n_item) break;
@@ -412,67 +477,104 @@ __global__ void __launch_bounds__(kThreads, 1) xengine_tc_kernel(TcParams p) {
             }
             fence_proxy_async_smem();   // operand stores -> visible to the tensor cores
             mbar_arrive(&bars.op_full[ob]);
-
-            if (st == n_stages - 1) {
-                // ---- epilogue of tile tl ----
-                if (!mbar_wait_bounded(&bars.acc_full, ph_acc, p.err, kErrXengineMmaTimeout)) {
-                    s_abort = 1;
-                    break;
-                }
-                ph_acc ^= 1u;
-                tc_fence_after();
-                // TMEM lane m holds row m of S; lanes 2j and 2j+1 are neighbours,
-                // so one shfl_down gives lane 2j the four terms of V[j][k].
-                const int m = quad * 32 + lane;
-                const int j = m >> 1;
-                const bool row_lane = ((lane & 1) == 0) && (m < 2 * N);
-                if (quad * 32 < 2 * N) {            // warp-uniform
-                    for (int c = 0; c < g.ct; ++c) {
-                        for (int cc = half; cc < nchunks; cc += 2) {
-                            float v[16], w[16];
-                            tmem_ld16(tmem + (static_cast<uint32_t>(quad * 32) << 16) +
-                                          static_cast<uint32_t>(c * g.n_mma + cc * 16),
-                                      v);
+        }
+    } else {
+        // ---------------------------- epilogue ----------------------------
+        const int et = tid - 32 - kConverters;
+        const int quad = warp & 3;             // TMEM lanes [32*quad, 32*quad+32)
+        const int nchunks = (2 * N + 15) / 16;
+        const int nq = g.ct / 2;                // float4 (two channels) per baseline
+        const int nblk = g.split ? 2 : 1;
+        for (int tl = 0; tl < my_tiles; ++tl) {
+            if (!mbar_wait_bounded(&bars.acc_full, static_cast<uint32_t>(tl) & 1u, p.err,
+                                   kErrXengineMmaTimeout, abort_flag)) {
+                s_abort = 1;
+                break;
+            }
+            tc_fence_after();
+            for (int c = 0; c < g.ct; ++c) {
+                for (int bk = 0; bk < nblk; ++bk) {
+                    // block = rows [lb, lb+2N) x columns [cb, cb+2N) of TMEM
+                    const bool isq = bk == 1;
+                    int lb = 0, cb = c * g.nb;
+                    if (g.form == kFp16Paired) {
+                        lb = (c & 1) * g.R;
+                        cb = (c >> 1) * g.nb + (c & 1) * g.R;
+                    } else if (isq && g.form == kSplitStacked) {
+                        lb = g.R;
+                    } else if (isq) {
+                        cb += g.R;   // wide split: T = P^T in columns [R, R+2N)
+                    }
+                    // warp-uniform: does this quarter hold any of the block's rows?
+                    if (quad * 32 + 32 <= lb || quad * 32 >= lb + 2 * N) continue;
+                    const int m = quad * 32 + lane - lb;
+                    const bool row_lane = ((m & 1) == 0) && m >= 0 && m < 2 * N;
+                    const int j = m >> 1;
+                    for (int cc = 0; cc < nchunks; ++cc) {
+                        float v[16], w[16];
+                        tmem_ld16(tmem + (static_cast<uint32_t>(quad * 32) << 16) +
+                                      static_cast<uint32_t>(cb + cc * 16),
+                                  v);
 #pragma unroll
-                            for (int i = 0; i < 16; ++i) w[i] = __shfl_down_sync(0xffffffffu, v[i], 1);
-                            if (row_lane) {
+                        for (int i = 0; i < 16; ++i) w[i] = __shfl_down_sync(0xffffffffu, v[i], 1);
+                        if (row_lane) {
 #pragma unroll
-                                for (int t = 0; t < 8; ++t) {
-                                    const int k = cc * 8 + t;
-                                    if (k >= j && k < N) {
-                                        // v = S[2j][*], w = S[2j+1][*]
-                                        const float re = v[2 * t] + w[2 * t + 1];
-                                        const float im = w[2 * t] - v[2 * t + 1];
+                            for (int t = 0; t < 8; ++t) {
+                                const int k = cc * 8 + t;
+                                // v = row 2j, w = row 2j+1
+                                const float re = (v[2 * t] + w[2 * t + 1]) * p.inv_scale2;
+                                const float im = (w[2 * t] - v[2 * t + 1]) * p.inv_scale2;
+                                if (k < N) {
+                                    if (isq) {
+                                        Qs[(j * N + k) * g.ct + c] = make_float2(re, im);
+                                    } else if (k >= j) {
                                         const int b = j * N - j * (j - 1) / 2 + (k - j);
-                                        Vs[b * g.ct + c] =
-                                            make_float2(re * p.inv_scale2, im * p.inv_scale2);
+                                        Vs[b * g.ct + c] = make_float2(re, im);
                                     }
                                 }
                             }
                         }
                     }
                 }
-                // accumulators read: the control warp may start the next tile
-                tc_fence_before();
-                mbar_arrive(&bars.acc_empty);
-                // all of V staged before anyone reads it back
-                mbar_arrive(&bars.epi);
-                if (!mbar_wait_bounded(&bars.epi, ph_epi, p.err, kErrXengineMmaTimeout)) {
-                    s_abort = 1;
-                    break;
+            }
+            // accumulators read: the MMAs of the next tile may start
+            tc_fence_before();
+            mbar_arrive(&bars.acc_empty);
+            mbar_arrive(&bars.epi);
+            if (!mbar_wait_bounded(&bars.epi, 0u, p.err, kErrXengineMmaTimeout, abort_flag)) {
+                s_abort = 1;
+                break;
+            }
+            // V (+ Q[j][k] + conj(Q[k][j])) into the row: this CTA is the only
+            // writer of these channels in this launch.
+            const int c0 = tile_c0(tl);
+            for (int q = et; q < n_baseline * nq; q += kEpilogue) {
+                const int b = q / nq;
+                const int c = (q - b * nq) * 2;
+                float2 v0 = Vs[b * g.ct + c], v1 = Vs[b * g.ct + c + 1];
+                if (g.split) {
+                    const int j = jk[b] >> 8, k = jk[b] & 0xff;
+                    const float2 *qa = Qs + (j * N + k) * g.ct + c;
+                    const float2 *qb = Qs + (k * N + j) * g.ct + c;
+                    v0.x += qa[0].x + qb[0].x;
+                    v0.y += qa[0].y - qb[0].y;
+                    v1.x += qa[1].x + qb[1].x;
+                    v1.y += qa[1].y - qb[1].y;
                 }
-                ph_epi ^= 1u;
-                const int c0 = tile_c0(tl);
-                // one owner per (baseline, channel) in this launch: fire-and-forget adds
-                for (int q = wt; q < n_baseline * g.ct; q += kWorkers) {
-                    const int b = q / g.ct;
-                    const int c = q - b * g.ct;
-                    float *dst = reinterpret_cast<float *>(
-                        p.acc + static_cast<size_t>(b) * p.n_freq + c0 + c);
-                    const float2 v = Vs[q];
-                    atomicAdd(dst, v.x);
-                    atomicAdd(dst + 1, v.y);
-                }
+                float4 *dst =
+                    reinterpret_cast<float4 *>(p.acc + static_cast<size_t>(b) * p.n_freq + c0 + c);
+                float4 a = *dst;
+                a.x += v0.x;
+                a.y += v0.y;
+                a.z += v1.x;
+                a.w += v1.y;
+                *dst = a;
+            }
+            // everyone done with Vs/Qs before the next tile overwrites them
+            mbar_arrive(&bars.epi);
+            if (!mbar_wait_bounded(&bars.epi, 1u, p.err, kErrXengineMmaTimeout, abort_flag)) {
+                s_abort = 1;
+                break;
             }
         }
     }
@@ -480,16 +582,16 @@ __global__ void __launch_bounds__(kThreads, 1) xengine_tc_kernel(TcParams p) {
     tc_fence_before();
     __syncthreads();
     if (s_abort && tid == 0) {
-        // Let every MMA and bulk copy this CTA issued land before TMEM and the
+        // Let every MMA and TMA load this CTA issued land before TMEM and the
         // CTA go away (bounded; the watchdog code is already recorded). A slot
-        // whose copy was consumed completed its phase; one still in flight
+        // whose load was consumed completed its phase; one still in flight
         // completes the phase after the last one consumed.
         umma_commit(&bars.fin);
         mbar_wait_bounded(&bars.fin, 0u, nullptr, 0);
-        for (int s = 0; s < n_ld; ++s) {
-            // copies issued into slot s (round robin from stage 0); the last
+        for (int s = 0; s < g.n_ld; ++s) {
+            // loads issued into slot s (round robin from stage 0); the last
             // one's completion is phase n_s - 1 of that slot's barrier
-            const uint32_t n_s = (s_ld_issued + n_ld - 1 - s) / n_ld;
+            const uint32_t n_s = (s_ld_issued + g.n_ld - 1 - s) / g.n_ld;
             if (n_s > 0) mbar_wait_bounded(&bars.load_full[s], (n_s - 1) & 1u, nullptr, 0);
         }
     }
@@ -508,23 +610,84 @@ int ilog2(int v) {
     return l;
 }
 
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+// (no link-time dependency on libcuda).
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(f);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
 } // namespace
 
-size_t xengine_tc_workspace_bytes(int, int) { return 0; }
+bool xengine_tc_shape_ok(int n_station, bool split, int ct, int kt) {
+    return make_geom(n_station, split, ct, kt).ok;
+}
 
-corr_status xengine_tc_launch(const XengineArgs &a, bool split, int num_sms,
+void xengine_tc_default_shape(int n_station, bool split, int *ct, int *kt) {
+    *kt = 16;
+    *ct = 0;
+    for (int c = 8; c >= 2; c /= 2) {
+        if (make_geom(n_station, split, c, 16).ok) {
+            *ct = c;
+            return;
+        }
+    }
+}
+
+corr_status xengine_tc_launch(const XengineArgs &a, bool split, int ct, int kt, int num_sms,
                               cudaStream_t stream) {
     if (a.frames <= 0) return CORR_OK;
-    const TcGeom g = make_geom(a.n_station, split);
-    if (g.smem > 227 * 1024)
-        return failf(CORR_ERR_INTERNAL, "tensor X-engine needs %d bytes of shared memory", g.smem);
+    const TcGeom g = make_geom(a.n_station, split, ct, kt);
+    if (!g.ok)
+        return failf(CORR_ERR_NOT_IMPL,
+                     "tensor X-engine: no %s tile of %d channels x %d frames for %d inputs",
+                     split ? "split" : "fp16", ct, kt, a.n_station);
     if (a.n_freq % g.ct != 0)
         return failf(CORR_ERR_ARG, "n_freq=%d is not a multiple of %d channels", a.n_freq, g.ct);
     if (a.y_frames < a.frames)
         return fail(CORR_ERR_INTERNAL, "spectra buffer shallower than the launch");
-    if (a.ytile != g.ct)
-        return failf(CORR_ERR_INTERNAL, "spectra tiles of %d channels, tensor engine tiles of %d",
+    if (a.ytile < g.ct || a.ytile % g.ct != 0 || a.n_freq % a.ytile != 0)
+        return failf(CORR_ERR_INTERNAL, "spectra tiles of %d channels, tensor tiles of %d",
                      a.ytile, g.ct);
+    if ((reinterpret_cast<uintptr_t>(a.acc) & 15) != 0)
+        return fail(CORR_ERR_ARG, "the tensor X-engine needs a 16-byte aligned accumulator");
+    EncodeTiledFn enc = encode_tiled();
+    if (enc == nullptr)
+        return fail(CORR_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    // spectra as a 4-D array of 8-byte elements, innermost first:
+    // (channel within its tile, station, frame, tile)
+    CUtensorMap map;
+    const cuuint64_t dims[4] = {static_cast<cuuint64_t>(a.ytile),
+                                static_cast<cuuint64_t>(a.n_station),
+                                static_cast<cuuint64_t>(a.y_frames),
+                                static_cast<cuuint64_t>(a.n_freq / a.ytile)};
+    const cuuint64_t row = static_cast<cuuint64_t>(a.ytile) * 8;
+    const cuuint64_t strides[3] = {row, row * a.n_station, row * a.n_station * a.y_frames};
+    const cuuint32_t box[4] = {static_cast<cuuint32_t>(g.ct), static_cast<cuuint32_t>(a.n_station),
+                               static_cast<cuuint32_t>(g.kt), 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult cr =
+        enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, const_cast<float2 *>(a.y), dims, strides, box,
+            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (cr != CUDA_SUCCESS)
+        return failf(CORR_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", static_cast<int>(cr));
     static int configured_smem = 0;
     if (configured_smem < g.smem) {
         corr_status st = cuda_check(
@@ -535,8 +698,7 @@ corr_status xengine_tc_launch(const XengineArgs &a, bool split, int num_sms,
         configured_smem = g.smem;
     }
     TcParams p{};
-    p.y = a.y;
-    p.y_frames = a.y_frames;
+    p.ytile = a.ytile;
     p.n_station = a.n_station;
     p.n_freq = a.n_freq;
     p.frames = a.frames;
@@ -548,7 +710,7 @@ corr_status xengine_tc_launch(const XengineArgs &a, bool split, int num_sms,
     p.g = g;
     const int n_tiles = a.n_freq / g.ct;
     const int grid = std::min(n_tiles, std::max(1, num_sms));
-    xengine_tc_kernel<<<grid, kThreads, g.smem, stream>>>(p);
+    xengine_tc_kernel<<<grid, kThreads, g.smem, stream>>>(map, p);
     return cuda_check(cudaGetLastError(), "xengine_tc_kernel launch");
 }
 

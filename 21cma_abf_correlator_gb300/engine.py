@@ -81,3 +81,21 @@ class FxEngine:
 
     def check(self) -> None:
         abi.check(self.lib.corrx_check(self.h), "corrx_check")
+
+    def tiles(self) -> dict:
+        """Current (ytile, xct, xkt): spectra tile width and tensor X tile shape."""
+        t = abi.corrx_tiles(struct_size=C.sizeof(abi.corrx_tiles))
+        abi.check(self.lib.corrx_get_tiles(self.h, C.byref(t)), "corrx_get_tiles")
+        return {"ytile": t.ytile, "xct": t.xct, "xkt": t.xkt}
+
+    def set_tiles(self, ytile: int, xct: int = 0, xkt: int = 0) -> None:
+        t = abi.corrx_tiles(struct_size=C.sizeof(abi.corrx_tiles), ytile=ytile, xct=xct, xkt=xkt)
+        abi.check(self.lib.corrx_set_tiles(self.h, C.byref(t)), "corrx_set_tiles")
+
+    def autotune(self, stream=None) -> dict:
+        """Time every feasible tile shape on this device; keep the fastest F+X pair."""
+        t = abi.corrx_tiles(struct_size=C.sizeof(abi.corrx_tiles))
+        abi.check(self.lib.corrx_autotune(self.h, C.c_void_p(_stream_handle(stream)), C.byref(t)),
+                  "corrx_autotune")
+        return {"ytile": t.ytile, "xct": t.xct, "xkt": t.xkt,
+                "ms_fengine": t.ms_fengine, "ms_xengine": t.ms_xengine}

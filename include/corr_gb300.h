@@ -56,7 +56,8 @@ corr_status corrx_destroy(void *eng);
  * If d_mask is not NULL, frame f of station s is treated as all zeros unless bit
  * (mask_bit0 + f) of the bit string at d_mask + s*mask_station_stride is set
  * (LSB first), exactly as the staging validity mask is read.
- * d_acc holds n_baseline*n_freq complex64 (FP32 re, im) and must not alias.
+ * d_acc holds n_baseline*n_freq complex64 (FP32 re, im), must not alias, and
+ * must be 16-byte aligned for the tensor X-engines.
  */
 corr_status corrx_accumulate(void *eng, const int8_t *d_samples, size_t station_stride,
                              size_t frame_stride, const uint8_t *d_mask,
@@ -69,6 +70,37 @@ corr_status corrx_scale(void *eng, void *d_acc, uint64_t frames, void *stream);
 /* Synchronise the engine's device and report a tripped device watchdog
    (CORR_ERR_INTERNAL) or a CUDA error. */
 corr_status corrx_check(void *eng);
+
+/*
+ * Tile shapes of an engine. ytile is the spectra layout between the F- and
+ * X-engines: n_freq = one contiguous row per (frame, station); a smaller power
+ * of two = channel tiles of that width holding every frame and station. xct and
+ * xkt are the tensor X-engine's channels per CTA tile (2, 4, 8) and frames per
+ * pipeline stage (16, 32); the plain X-engine ignores them. corrx_create picks
+ * contiguous rows and the widest feasible tensor tile with 16-frame stages.
+ */
+typedef struct corrx_tiles {
+    uint32_t struct_size; /* sizeof(corrx_tiles)                                   */
+    int32_t  ytile;
+    int32_t  xct;
+    int32_t  xkt;
+    float    ms_fengine;  /* corrx_autotune: F-engine ms per max_frames pass       */
+    float    ms_xengine;  /* corrx_autotune: X-engine ms per max_frames pass       */
+} corrx_tiles;
+
+corr_status corrx_get_tiles(void *eng, corrx_tiles *out);
+/* CORR_ERR_ARG for an infeasible shape; the spectra buffer's previous contents
+   become meaningless (run the F-engine again). */
+corr_status corrx_set_tiles(void *eng, const corrx_tiles *t);
+/* Time every feasible (ytile, xct, xkt) on this device -- one F-engine and one
+   X-engine pass of max_frames synthetic frames each (temporary device buffers of
+   n_station*max_frames*2*n_freq bytes plus one row) -- keep the fastest F+X
+   pair and report it in *out (may be NULL). Synchronises `stream`. */
+corr_status corrx_autotune(void *eng, void *stream, corrx_tiles *out);
+
+/* corrx_autotune for the engine inside an ABI context; allowed only while no
+   row holds data, like corr_set_xengine. */
+corr_status corr_autotune(void *ctx, corrx_tiles *out);
 
 /* The two halves of corrx_accumulate, for timing and profiling each kernel on
    its own. corrx_run_fengine transforms `frames` (<= max_frames) frames into the
