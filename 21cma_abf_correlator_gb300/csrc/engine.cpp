@@ -344,7 +344,7 @@ corr_status fxplan_autotune(FxPlan *p, cudaStream_t stream, corrx_tiles *out) {
     } else {
         const bool split = p->xmode == CORR_X_TC_FP16_SPLIT;
         for (int ct = 8; ct >= 2; ct /= 2)
-            for (int kt = 16; kt <= 32; kt *= 2)
+            for (int kt = 16; kt <= 64; kt *= 2)
                 if (xengine_tc_shape_ok(p->n_station, split, ct, kt)) {
                     cands.push_back({p->n_freq, ct, kt});
                     if (ct < p->n_freq) cands.push_back({ct, ct, kt});

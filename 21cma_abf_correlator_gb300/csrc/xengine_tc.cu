@@ -40,11 +40,14 @@
 //
 // Warp-specialised persistent CTAs, one per SM (TMEM), CT channels per tile:
 //   warp 0 (lane 0): TMA tensor loads -- one 4-D box {CT channels, N stations,
-//     KT frames, 1 tile} of the spectra per stage, into a ring as deep as shared
-//     memory allows -- and the MMAs of a stage once its operands are written.
-//   warps 1-8 (converters): scale, round and split a landed stage into the
+//     KT frames, 1 tile} of the spectra per stage (3-D, KT rows of CT*N, when
+//     the spectra tiles are CT wide) into a ring as deep as shared memory allows.
+//     The map ends at the launch's last frame, so a partial stage arrives
+//     zero-padded.
+//   warp 1 (lane 0): the MMAs of a stage once its operands are written.
+//   warps 2-9 (converters): scale, round and split a landed stage into the
 //     K-major no-swizzle operand layout (8-row x 16-byte core matrices).
-//   warps 9-12 (epilogue, one per TMEM lane quarter): after a tile's last MMA,
+//   warps 10-13 (epilogue, one per TMEM lane quarter): after a tile's last MMA,
 //     read the accumulators (tcgen05.ld), pair rows 2j/2j+1 with one shuffle,
 //     stage V (and Q), release TMEM, then add V into the row in global memory
 //     with 16-byte read-modify-writes (one owner per channel tile and launch).
@@ -63,9 +66,11 @@
 namespace corrgb {
 namespace {
 
-constexpr int kConverters = 256;                 // warps 1-8
-constexpr int kEpilogue = 128;                   // warps 9-12
-constexpr int kThreads = 32 + kConverters + kEpilogue;
+constexpr int kConverters = 256;                 // warps 2-9
+constexpr int kEpilogue = 128;                   // warps 10-13
+constexpr int kThreads = 64 + kConverters + kEpilogue;
+constexpr int kFirstConverterWarp = 2;
+constexpr int kFirstEpilogueWarp = kFirstConverterWarp + kConverters / 32;
 constexpr int kMaxLoadStages = 6;
 constexpr int kMaxOpStages = 3;
 constexpr int kMaxItems = 4;                     // conversion items per converter thread
@@ -85,12 +90,14 @@ struct TcGeom {
     int sbo;           // bytes between 8-row groups = (kt/8) * 128
     int region_stride; // bytes between regions (multiple of 128, one 128-byte pad)
     int tmem_cols;
+    int acc_cols;      // TMEM columns of one accumulator set (a tile)
+    int n_acc;         // accumulator sets (2 = the next tile's MMAs overlap the epilogue)
     int op_stage;      // operand bytes per stage
     int ld_stage;      // fp32 bytes per stage = kt * N * ct * 8
     int n_ld;
     int n_op;
-    int vs_bytes;      // staged V: n_baseline x ct float2
-    int qs_bytes;      // staged Q: N*N x ct float2 (split forms)
+    int vs_bytes;      // staged V: ct planes of n_baseline float2, k-major triangle
+    int qs_bytes;      // staged Q: ct planes of N*N float2, [k][j] (split forms)
     int smem;
     int items;         // conversion items per stage = ct * N * kt/8
     bool ok;
@@ -112,7 +119,8 @@ TcGeom make_geom(int n_station, bool split, int ct, int kt) {
     g.ct = ct;
     g.kt = kt;
     const int N = n_station;
-    if (N < 1 || N > 64 || (kt != 16 && kt != 32) || ct < 2 || ct > 8 || (ct & (ct - 1)))
+    if (N < 1 || N > 64 || (kt != 16 && kt != 32 && kt != 64) || ct < 2 || ct > 8 ||
+        (ct & (ct - 1)))
         return g;
     g.R = round_up(2 * N, 8);
     int rows_valid;
@@ -136,9 +144,13 @@ TcGeom make_geom(int n_station, bool split, int ct, int kt) {
     if (g.form == kSplitWide) max_col = std::max(max_col, (ct - 1) * g.nb + g.R + chunk);
     if (g.form == kFp16Paired)
         max_col = std::max(max_col, (g.regions - 1) * g.nb + g.R + chunk);
+    if (max_col > 512) return g;
+    g.acc_cols = round_up(max_col, 32);
+    // Two accumulator sets when they fit: tile t+1 accumulates while the
+    // epilogue still reads tile t.
+    g.n_acc = 2 * g.acc_cols <= 512 ? 2 : 1;
     int cols = 32;
-    while (cols < max_col) cols *= 2;
-    if (cols > 512) return g;
+    while (cols < g.n_acc * g.acc_cols) cols *= 2;
     g.tmem_cols = cols;
     g.sbo = (kt / 8) * 128;
     const int groups = (rows_valid + 7) / 8;
@@ -211,8 +223,8 @@ __device__ __forceinline__ void tc_fence_before() {
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
-    uint32_t r[16];
+// Issue a 32-lane x 16-column TMEM load without waiting (tmem_ld_wait completes it).
+__device__ __forceinline__ void tmem_ld16_issue(uint32_t taddr, uint32_t *r) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
         "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
@@ -221,9 +233,10 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
           "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(taddr)
         : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld_wait() {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 // 4-D TMA tile load global -> shared, completing on `bar`.
@@ -237,12 +250,23 @@ __device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, i
         : "memory");
 }
 
+// 3-D TMA tile load global -> shared, completing on `bar`.
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z,
+                                            uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+        : "memory");
+}
+
 __device__ __forceinline__ uint32_t half2_bits(__half2 h) {
     return *reinterpret_cast<const uint32_t *>(&h);
 }
 
 struct TcParams {
     int ytile;
+    int merged;        // ytile == ct: the map is (ct*N, frame, tile), one row per frame
     int n_station;
     int n_freq;
     int frames;
@@ -255,10 +279,11 @@ struct TcParams {
 
 struct TcBars {
     uint64_t load_full[kMaxLoadStages];  // a stage's TMA load landed (tx-count)
+    uint64_t load_empty[kMaxLoadStages]; // converters finished reading a slot (256 arrivals)
     uint64_t op_full[kMaxOpStages];      // converters wrote a stage's operands (256 arrivals)
     uint64_t op_empty[kMaxOpStages];     // MMAs reading an operand buffer finished (commit)
-    uint64_t acc_full;                   // a tile's MMAs finished (commit)
-    uint64_t acc_empty;                  // epilogue read the accumulators (128 arrivals)
+    uint64_t acc_full[2];                // a tile's MMAs finished (commit), per set
+    uint64_t acc_empty[2];               // epilogue read a set (128 arrivals)
     uint64_t epi;                        // epilogue-only sync (128 arrivals, twice per tile)
     uint64_t fin;                        // abort path: every MMA this CTA issued finished
 };
@@ -304,13 +329,18 @@ __global__ void __launch_bounds__(kThreads, 1)
         jk[b] = static_cast<uint16_t>((j << 8) | (j + rem));
     }
     if (tid == 0) {
-        for (int s = 0; s < g.n_ld; ++s) mbar_init(&bars.load_full[s], 1);
+        for (int s = 0; s < g.n_ld; ++s) {
+            mbar_init(&bars.load_full[s], 1);
+            mbar_init(&bars.load_empty[s], kConverters);
+        }
         for (int s = 0; s < g.n_op; ++s) {
             mbar_init(&bars.op_full[s], kConverters);
             mbar_init(&bars.op_empty[s], 1);
         }
-        mbar_init(&bars.acc_full, 1);
-        mbar_init(&bars.acc_empty, kEpilogue);
+        for (int s = 0; s < 2; ++s) {
+            mbar_init(&bars.acc_full[s], 1);
+            mbar_init(&bars.acc_empty[s], kEpilogue);
+        }
         mbar_init(&bars.epi, kEpilogue);
         mbar_init(&bars.fin, 1);
         s_abort = 0;
@@ -335,32 +365,54 @@ __global__ void __launch_bounds__(kThreads, 1)
     };
 
     if (warp == 0) {
-        // ------------------------- loads + MMAs -------------------------
+        // ---------------------------- TMA loads ----------------------------
         if (lane == 0) {
             asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&ymap))
                          : "memory");
-            auto issue = [&](int gs) {
+            for (int gs = 0; gs < total && *abort_flag == 0; ++gs) {
                 const int tl = gs / n_stages;
                 const int st = gs - tl * n_stages;
                 const int slot = gs % g.n_ld;
+                const int use = gs / g.n_ld;
+                if (use > 0 &&
+                    !mbar_wait_bounded(&bars.load_empty[slot], static_cast<uint32_t>(use - 1) & 1u,
+                                       p.err, kErrXengineMmaTimeout, abort_flag)) {
+                    s_abort = 1;
+                    break;
+                }
                 const int c0 = tile_c0(tl);
                 mbar_arrive_expect_tx(&bars.load_full[slot], static_cast<uint32_t>(g.ld_stage));
-                // frames past the buffer's end arrive as zeros; frames in
-                // [frames, y_frames) are stale and the converters zero them
-                tma_load_4d(ld_ring + slot * g.ld_stage, &ymap, c0 & (p.ytile - 1), 0, st * g.kt,
-                            c0 / p.ytile, &bars.load_full[slot]);
+                // frames past `frames` (the map's last frame) arrive as zeros
+                if (p.merged)
+                    tma_load_3d(ld_ring + slot * g.ld_stage, &ymap, 0, st * g.kt, c0 / p.ytile,
+                                &bars.load_full[slot]);
+                else
+                    tma_load_4d(ld_ring + slot * g.ld_stage, &ymap, c0 & (p.ytile - 1), 0,
+                                st * g.kt, c0 / p.ytile, &bars.load_full[slot]);
                 ++s_ld_issued;
-            };
-            for (int gs = 0; gs < g.n_ld && gs < total; ++gs) issue(gs);
+            }
+        }
+    } else if (warp == 1) {
+        // ------------------------------ MMAs ------------------------------
+        if (lane == 0) {
             const uint32_t idesc = instr_desc_f16_f32(128, g.nb);
             const int ksteps = g.kt / 16;
+            // Descriptors differ only in their start-address field, which
+            // cannot carry: (address >> 4) of shared memory fits its 14 bits.
+            const uint64_t desc0 = smem_desc(smem_addr(op_ring), g.sbo);
+            uint32_t roff[8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+                roff[r] = static_cast<uint32_t>(r * g.region_stride + region_skew(r)) >> 4;
             for (int gs = 0; gs < total && *abort_flag == 0; ++gs) {
                 const int tl = gs / n_stages;
                 const int st = gs - tl * n_stages;
                 const int ob = gs % g.n_op;
-                if (st == 0 && tl > 0) {
-                    // the previous tile's accumulators must be read before overwrite
-                    if (!mbar_wait_bounded(&bars.acc_empty, static_cast<uint32_t>(tl - 1) & 1u,
+                const int aset = tl % g.n_acc;
+                const int use = tl / g.n_acc;   // earlier tiles that used this set
+                if (st == 0 && use > 0) {
+                    // this set's previous tile must be read before it is overwritten
+                    if (!mbar_wait_bounded(&bars.acc_empty[aset], static_cast<uint32_t>(use - 1) & 1u,
                                            p.err, kErrXengineMmaTimeout, abort_flag)) {
                         s_abort = 1;
                         break;
@@ -372,36 +424,34 @@ __global__ void __launch_bounds__(kThreads, 1)
                     break;
                 }
                 tc_fence_after();
-                const uint32_t base = smem_addr(op_ring + ob * g.op_stage);
-                for (int r = 0; r < g.regions; ++r) {
-                    const uint32_t rb = base + r * g.region_stride + region_skew(r);
-                    const uint32_t d = tmem + static_cast<uint32_t>(r * g.nb);
+                const uint64_t dstage = desc0 + (static_cast<uint32_t>(ob * g.op_stage) >> 4);
+                const uint32_t dset = tmem + static_cast<uint32_t>(aset * g.acc_cols);
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    if (r >= g.regions) break;
+                    const uint32_t d = dset + static_cast<uint32_t>(r * g.nb);
+                    const uint64_t dr = dstage + roff[r];
                     for (int ks = 0; ks < ksteps; ++ks) {
-                        const uint64_t desc = smem_desc(rb + ks * 2 * kLBO, g.sbo);
+                        const uint64_t desc = dr + static_cast<uint32_t>(ks * 2 * kLBO / 16);
                         umma_f16(d, desc, desc, idesc, (st > 0 || ks > 0) ? 1u : 0u);
                     }
                 }
                 umma_commit(&bars.op_empty[ob]);
-                if (st == n_stages - 1) umma_commit(&bars.acc_full);
-                // op_full for this stage means every converter has read its
-                // fp32 slot: refill the slot n_ld stages ahead.
-                if (gs + g.n_ld < total) issue(gs + g.n_ld);
+                if (st == n_stages - 1) umma_commit(&bars.acc_full[aset]);
             }
         }
-    } else if (warp <= kConverters / 32) {
+    } else if (warp < kFirstEpilogueWarp) {
         // --------------------------- converters ---------------------------
-        const int wt = tid - 32;
+        const int wt = tid - 32 * kFirstConverterWarp;
         // This thread's items (channel c, station s, 8-frame group kq) are the
-        // same every stage: keep their fp32 offsets, operand offsets, frames.
+        // same every stage: keep their fp32 and operand offsets.
         int n_item = 0;
         uint32_t it_ld[kMaxItems], it_op[kMaxItems];
-        int it_f[kMaxItems];
         const int lo_off = (g.R / 8) * g.sbo;   // Dl rows start at row R
 #pragma unroll
         for (int i = 0; i < kMaxItems; ++i) {
             it_ld[i] = 0;
             it_op[i] = 0;
-            it_f[i] = 0;
             const int q = wt + i * kConverters;
             if (q < g.items) {
                 const int c = q % g.ct;
@@ -416,14 +466,11 @@ __global__ void __launch_bounds__(kThreads, 1)
                 it_ld[i] = static_cast<uint32_t>((kq * 8 * N + s) * g.ct + c);
                 it_op[i] = static_cast<uint32_t>(region * g.region_stride + region_skew(region) +
                                                  (row >> 3) * g.sbo + kq * kLBO + (row & 7) * 16);
-                it_f[i] = kq * 8;
                 n_item = i + 1;
             }
         }
         const int row_step = N * g.ct;   // float2 between consecutive frames of a slot
         for (int gs = 0; gs < total; ++gs) {
-            const int tl = gs / n_stages;
-            const int st = gs - tl * n_stages;
             const int lb = gs % g.n_ld;
             const int ob = gs % g.n_op;
             bool ok = mbar_wait_bounded(&bars.load_full[lb], static_cast<uint32_t>(gs / g.n_ld) & 1u,
@@ -439,19 +486,16 @@ __global__ void __launch_bounds__(kThreads, 1)
             // fp32 slot: [frame][station][CT channels]
             const float2 *ld = reinterpret_cast<const float2 *>(ld_ring + lb * g.ld_stage);
             unsigned char *op = op_ring + ob * g.op_stage;
-            const int f0 = st * g.kt;
 #pragma unroll
             for (int it = 0; it < kMaxItems; ++it) {
                 if (it >= n_item) break;
                 const float2 *src = ld + it_ld[it];
-                const int fb = f0 + it_f[it];
                 uint32_t hre[4], him[4], lre[4], lim[4];
 #pragma unroll
                 for (int i = 0; i < 4; ++i) {
-                    float2 va = src[(2 * i) * row_step];
-                    float2 vb = src[(2 * i + 1) * row_step];
-                    if (fb + 2 * i >= p.frames) va = make_float2(0.f, 0.f);
-                    if (fb + 2 * i + 1 >= p.frames) vb = make_float2(0.f, 0.f);
+                    // frames past `frames` arrived as zeros (the tensor map ends there)
+                    const float2 va = src[(2 * i) * row_step];
+                    const float2 vb = src[(2 * i + 1) * row_step];
                     const float a0 = va.x * p.scale, a1 = vb.x * p.scale;
                     const float b0 = va.y * p.scale, b1 = vb.y * p.scale;
                     const __half2 hr = __floats2half2_rn(a0, a1);
@@ -475,26 +519,34 @@ __global__ void __launch_bounds__(kThreads, 1)
                         make_uint4(lim[0], lim[1], lim[2], lim[3]);
                 }
             }
+            mbar_arrive(&bars.load_empty[lb]);   // the fp32 slot may be refilled
             fence_proxy_async_smem();   // operand stores -> visible to the tensor cores
             mbar_arrive(&bars.op_full[ob]);
         }
     } else {
         // ---------------------------- epilogue ----------------------------
-        const int et = tid - 32 - kConverters;
+        const int et = tid - 32 * kFirstEpilogueWarp;
         const int quad = warp & 3;             // TMEM lanes [32*quad, 32*quad+32)
         const int nchunks = (2 * N + 15) / 16;
         const int nq = g.ct / 2;                // float4 (two channels) per baseline
         const int nblk = g.split ? 2 : 1;
+        // Staging, one plane per channel, j fastest so that the row lanes of a
+        // warp (consecutive j) store to consecutive addresses:
+        //   Vt[c][k(k+1)/2 + j] = V[j][k] (j <= k),  Qs[c][k][j] = Q[j][k].
+        const int plane_v = n_baseline;
         for (int tl = 0; tl < my_tiles; ++tl) {
-            if (!mbar_wait_bounded(&bars.acc_full, static_cast<uint32_t>(tl) & 1u, p.err,
-                                   kErrXengineMmaTimeout, abort_flag)) {
+            const int aset = tl % g.n_acc;
+            if (!mbar_wait_bounded(&bars.acc_full[aset], static_cast<uint32_t>(tl / g.n_acc) & 1u,
+                                   p.err, kErrXengineMmaTimeout, abort_flag)) {
                 s_abort = 1;
                 break;
             }
             tc_fence_after();
+            const uint32_t tbase = tmem + (static_cast<uint32_t>(quad * 32) << 16) +
+                                   static_cast<uint32_t>(aset * g.acc_cols);
             for (int c = 0; c < g.ct; ++c) {
                 for (int bk = 0; bk < nblk; ++bk) {
-                    // block = rows [lb, lb+2N) x columns [cb, cb+2N) of TMEM
+                    // block = rows [lb, lb+2N) x columns [cb, cb+2N) of the set
                     const bool isq = bk == 1;
                     int lb = 0, cb = c * g.nb;
                     if (g.form == kFp16Paired) {
@@ -510,26 +562,35 @@ __global__ void __launch_bounds__(kThreads, 1)
                     const int m = quad * 32 + lane - lb;
                     const bool row_lane = ((m & 1) == 0) && m >= 0 && m < 2 * N;
                     const int j = m >> 1;
-                    for (int cc = 0; cc < nchunks; ++cc) {
-                        float v[16], w[16];
-                        tmem_ld16(tmem + (static_cast<uint32_t>(quad * 32) << 16) +
-                                      static_cast<uint32_t>(cb + cc * 16),
-                                  v);
+                    // up to four 16-column chunks per TMEM wait
+                    for (int c0 = 0; c0 < nchunks; c0 += 4) {
+                        uint32_t r[4][16];
 #pragma unroll
-                        for (int i = 0; i < 16; ++i) w[i] = __shfl_down_sync(0xffffffffu, v[i], 1);
-                        if (row_lane) {
+                        for (int q = 0; q < 4; ++q)
+                            if (c0 + q < nchunks) tmem_ld16_issue(tbase + cb + (c0 + q) * 16, r[q]);
+                        tmem_ld_wait();
 #pragma unroll
-                            for (int t = 0; t < 8; ++t) {
-                                const int k = cc * 8 + t;
-                                // v = row 2j, w = row 2j+1
-                                const float re = (v[2 * t] + w[2 * t + 1]) * p.inv_scale2;
-                                const float im = (w[2 * t] - v[2 * t + 1]) * p.inv_scale2;
-                                if (k < N) {
-                                    if (isq) {
-                                        Qs[(j * N + k) * g.ct + c] = make_float2(re, im);
-                                    } else if (k >= j) {
-                                        const int b = j * N - j * (j - 1) / 2 + (k - j);
-                                        Vs[b * g.ct + c] = make_float2(re, im);
+                        for (int q = 0; q < 4; ++q) {
+                            if (c0 + q >= nchunks) break;
+                            float v[16], w[16];
+#pragma unroll
+                            for (int i = 0; i < 16; ++i) {
+                                v[i] = __uint_as_float(r[q][i]);
+                                w[i] = __shfl_down_sync(0xffffffffu, v[i], 1);
+                            }
+                            if (row_lane) {
+#pragma unroll
+                                for (int t = 0; t < 8; ++t) {
+                                    const int k = (c0 + q) * 8 + t;
+                                    // v = row 2j, w = row 2j+1
+                                    const float re = (v[2 * t] + w[2 * t + 1]) * p.inv_scale2;
+                                    const float im = (w[2 * t] - v[2 * t + 1]) * p.inv_scale2;
+                                    if (k < N) {
+                                        if (isq)
+                                            Qs[(c * N + k) * N + j] = make_float2(re, im);
+                                        else if (k >= j)
+                                            Vs[c * plane_v + k * (k + 1) / 2 + j] =
+                                                make_float2(re, im);
                                     }
                                 }
                             }
@@ -537,9 +598,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                     }
                 }
             }
-            // accumulators read: the MMAs of the next tile may start
+            // this set is read: the MMAs of tile tl + n_acc may start
             tc_fence_before();
-            mbar_arrive(&bars.acc_empty);
+            mbar_arrive(&bars.acc_empty[aset]);
             mbar_arrive(&bars.epi);
             if (!mbar_wait_bounded(&bars.epi, 0u, p.err, kErrXengineMmaTimeout, abort_flag)) {
                 s_abort = 1;
@@ -551,15 +612,17 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int q = et; q < n_baseline * nq; q += kEpilogue) {
                 const int b = q / nq;
                 const int c = (q - b * nq) * 2;
-                float2 v0 = Vs[b * g.ct + c], v1 = Vs[b * g.ct + c + 1];
+                const int j = jk[b] >> 8, k = jk[b] & 0xff;
+                const int tri = k * (k + 1) / 2 + j;
+                float2 v0 = Vs[c * plane_v + tri], v1 = Vs[(c + 1) * plane_v + tri];
                 if (g.split) {
-                    const int j = jk[b] >> 8, k = jk[b] & 0xff;
-                    const float2 *qa = Qs + (j * N + k) * g.ct + c;
-                    const float2 *qb = Qs + (k * N + j) * g.ct + c;
-                    v0.x += qa[0].x + qb[0].x;
-                    v0.y += qa[0].y - qb[0].y;
-                    v1.x += qa[1].x + qb[1].x;
-                    v1.y += qa[1].y - qb[1].y;
+                    const float2 qa0 = Qs[(c * N + k) * N + j], qb0 = Qs[(c * N + j) * N + k];
+                    const float2 qa1 = Qs[((c + 1) * N + k) * N + j];
+                    const float2 qb1 = Qs[((c + 1) * N + j) * N + k];
+                    v0.x += qa0.x + qb0.x;
+                    v0.y += qa0.y - qb0.y;
+                    v1.x += qa1.x + qb1.x;
+                    v1.y += qa1.y - qb1.y;
                 }
                 float4 *dst =
                     reinterpret_cast<float4 *>(p.acc + static_cast<size_t>(b) * p.n_freq + c0 + c);
@@ -581,13 +644,17 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     tc_fence_before();
     __syncthreads();
-    if (s_abort && tid == 0) {
-        // Let every MMA and TMA load this CTA issued land before TMEM and the
-        // CTA go away (bounded; the watchdog code is already recorded). A slot
-        // whose load was consumed completed its phase; one still in flight
-        // completes the phase after the last one consumed.
+    if (s_abort && tid == 32) {
+        // Let every MMA this CTA issued finish before TMEM goes away (bounded;
+        // the watchdog code is already recorded). A commit covers the issuing
+        // thread's earlier MMAs.
         umma_commit(&bars.fin);
         mbar_wait_bounded(&bars.fin, 0u, nullptr, 0);
+    }
+    if (s_abort && tid == 0) {
+        // Let every TMA load land before the CTA's shared memory goes away. A
+        // slot whose load was consumed completed its phase; one still in flight
+        // completes the phase after the last one consumed.
         for (int s = 0; s < g.n_ld; ++s) {
             // loads issued into slot s (round robin from stage 0); the last
             // one's completion is phase n_s - 1 of that slot's barrier
@@ -640,14 +707,17 @@ bool xengine_tc_shape_ok(int n_station, bool split, int ct, int kt) {
 }
 
 void xengine_tc_default_shape(int n_station, bool split, int *ct, int *kt) {
-    *kt = 16;
+    // 32-frame stages halve the per-stage handoffs of 16-frame ones; then the
+    // widest tile that fits.
     *ct = 0;
-    for (int c = 8; c >= 2; c /= 2) {
-        if (make_geom(n_station, split, c, 16).ok) {
-            *ct = c;
-            return;
-        }
-    }
+    *kt = 0;
+    for (int k : {32, 16})
+        for (int c = 8; c >= 2; c /= 2)
+            if (make_geom(n_station, split, c, k).ok) {
+                *ct = c;
+                *kt = k;
+                return;
+            }
 }
 
 corr_status xengine_tc_launch(const XengineArgs &a, bool split, int ct, int kt, int num_sms,
@@ -670,22 +740,38 @@ corr_status xengine_tc_launch(const XengineArgs &a, bool split, int ct, int kt, 
     EncodeTiledFn enc = encode_tiled();
     if (enc == nullptr)
         return fail(CORR_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-    // spectra as a 4-D array of 8-byte elements, innermost first:
-    // (channel within its tile, station, frame, tile)
+    // Spectra as 8-byte elements, innermost first. Tiles as wide as the tensor
+    // tile: (channel*station, frame, tile) -- a stage is KT rows of CT*N
+    // contiguous elements. Wider tiles (contiguous rows when ytile = n_freq):
+    // (channel within tile, station, frame, tile), KT*N rows of CT elements.
     CUtensorMap map;
-    const cuuint64_t dims[4] = {static_cast<cuuint64_t>(a.ytile),
-                                static_cast<cuuint64_t>(a.n_station),
-                                static_cast<cuuint64_t>(a.y_frames),
-                                static_cast<cuuint64_t>(a.n_freq / a.ytile)};
+    const bool merged = a.ytile == g.ct && g.ct * a.n_station <= 256;
     const cuuint64_t row = static_cast<cuuint64_t>(a.ytile) * 8;
-    const cuuint64_t strides[3] = {row, row * a.n_station, row * a.n_station * a.y_frames};
-    const cuuint32_t box[4] = {static_cast<cuuint32_t>(g.ct), static_cast<cuuint32_t>(a.n_station),
-                               static_cast<cuuint32_t>(g.kt), 1};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
-    const CUresult cr =
-        enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, const_cast<float2 *>(a.y), dims, strides, box,
-            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    CUresult cr;
+    if (merged) {
+        const cuuint64_t dims[3] = {static_cast<cuuint64_t>(a.ytile) * a.n_station,
+                                    static_cast<cuuint64_t>(a.frames),
+                                    static_cast<cuuint64_t>(a.n_freq / a.ytile)};
+        const cuuint64_t strides[2] = {row * a.n_station, row * a.n_station * a.y_frames};
+        const cuuint32_t box[3] = {static_cast<cuuint32_t>(g.ct * a.n_station),
+                                   static_cast<cuuint32_t>(g.kt), 1};
+        cr = enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<float2 *>(a.y), dims, strides,
+                 box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    } else {
+        const cuuint64_t dims[4] = {static_cast<cuuint64_t>(a.ytile),
+                                    static_cast<cuuint64_t>(a.n_station),
+                                    static_cast<cuuint64_t>(a.frames),
+                                    static_cast<cuuint64_t>(a.n_freq / a.ytile)};
+        const cuuint64_t strides[3] = {row, row * a.n_station, row * a.n_station * a.y_frames};
+        const cuuint32_t box[4] = {static_cast<cuuint32_t>(g.ct),
+                                   static_cast<cuuint32_t>(a.n_station),
+                                   static_cast<cuuint32_t>(g.kt), 1};
+        cr = enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, const_cast<float2 *>(a.y), dims, strides,
+                 box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    }
     if (cr != CUDA_SUCCESS)
         return failf(CORR_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", static_cast<int>(cr));
     static int configured_smem = 0;
@@ -699,6 +785,7 @@ corr_status xengine_tc_launch(const XengineArgs &a, bool split, int ct, int kt, 
     }
     TcParams p{};
     p.ytile = a.ytile;
+    p.merged = merged ? 1 : 0;
     p.n_station = a.n_station;
     p.n_freq = a.n_freq;
     p.frames = a.frames;

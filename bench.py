@@ -205,6 +205,8 @@ def main() -> None:
                     help="override frames per integration (smaller cases for profiling)")
     ap.add_argument("--pass-frames", type=int, default=PASS_FRAMES,
                     help="frames per F/X pass (spectra buffer depth)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep the default tile shapes instead of autotuning them")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the batching and stream workloads")
     args = ap.parse_args()
@@ -240,9 +242,12 @@ def main() -> None:
     modes = {"plain": abi.CORR_X_PLAIN_FP32, "tc": abi.CORR_X_TC_FP16,
              "tc_split": abi.CORR_X_TC_FP16_SPLIT}
     if args.xmode == "auto":
-        candidates = ["tc_split", "plain"]
+        candidates = ["tc_split", "tc", "plain"]
     else:
         candidates = [args.xmode]
+    # per-visibility error bound each path is tested to (vs the float64 oracle):
+    # plain and split 1e-5 / 2e-5 at any length; FP16 6e-3/sqrt(frames)
+    err_bound = {"plain": 1e-5, "tc_split": 2e-5, "tc": 6e-3 / math.sqrt(F)}
 
     x, mask = synth.generate_torch(w, F, seed_offset=rank)
     torch.cuda.synchronize()
@@ -258,9 +263,11 @@ def main() -> None:
 
     results = {}
     engines = {}
+    tiles = {}
     for name in candidates:
         try:
             eng = pkg.FxEngine(N, nf, PASS_FRAMES, xmode=modes[name])
+            tiles[name] = eng.autotune(stream) if not args.no_tune else eng.tiles()
             acc = eng.new_acc()
             step = make_step(eng, acc)
             step()
@@ -291,11 +298,13 @@ def main() -> None:
             torch.distributed.barrier()
         return e0.elapsed_time(e1) / k
 
-    # pick the headline path: the fastest available X-engine
+    # the headline path: the fastest X-engine whose tested error bound meets the
+    # 1e-4 precision target at this integration length
     per_path = {}
     for name, (eng, acc, step) in engines.items():
         per_path[name] = time_steps(step, 2, 1)
-    best = min(per_path, key=per_path.get)
+    eligible = [n for n in per_path if err_bound[n] <= 1e-4] or list(per_path)
+    best = min(eligible, key=per_path.get)
     eng, acc, step = engines[best]
 
     sampler = ClockSampler(local)
@@ -314,7 +323,9 @@ def main() -> None:
     paths = {}
     for name, (e_, a_, s_) in engines.items():
         m = ms if name == best else time_steps(s_, max(2, args.steps // 2), 1)
-        paths[name] = {"value": samples_step / (m * 1e-3) / 1e9, "ms_per_step": m}
+        paths[name] = {"value": samples_step / (m * 1e-3) / 1e9, "ms_per_step": m,
+                       "tiles": {k: tiles[name][k] for k in ("ytile", "xct", "xkt")},
+                       "per_vis_err_bound": err_bound[name]}
 
     # per-kernel times: one pass of PASS_FRAMES frames through each kernel alone
     hbm_peak, _, peak_kind = peaks()
@@ -360,7 +371,8 @@ def main() -> None:
     dk = kernels[dom]
     roofline = {"kernel": dom, "bound": "hbm", "achieved": dk["achieved_gbs"],
                 "peak": hbm_peak, "unit": "GB/s", "frac": dk["achieved_gbs"] / hbm_peak,
-                "peak_kind": peak_kind, "traffic": None,
+                "peak_kind": peak_kind,
+                "traffic": ncu_traffic(dom, w.name, PASS_FRAMES),
                 "alg_bytes_per_launch": dk["alg_bytes"], "frames_per_launch": PASS_FRAMES}
 
     e2e = None
@@ -373,7 +385,10 @@ def main() -> None:
             e_[0].close()
         del x, mask
         torch.cuda.empty_cache()
-        extra["batching"] = run_batching(pkg, synth, torch, modes[best], stream)
+        # the shortest batching block (512 frames) must still meet 1e-4
+        bmode = best if best != "tc" or 6e-3 / math.sqrt(512) <= 1e-4 else "tc_split"
+        extra["batching"] = run_batching(pkg, synth, torch, modes[bmode], stream)
+        extra["batching"]["xengine"] = bmode
         torch.cuda.empty_cache()
         extra["stream"] = run_stream(pkg, synth, torch, stream)
         torch.cuda.empty_cache()
@@ -394,6 +409,7 @@ def main() -> None:
             "data": "synthetic (seeded Gaussian + common signal, delays; generated in HBM)",
             "config": {"workload": w.name, "n_station": N, "n_freq": nf,
                        "frames_per_integration": F, "baselines": B, "xengine": best,
+                       "tiles": paths[best]["tiles"],
                        "frames_per_pass": PASS_FRAMES, "parallelism": f"replicas x{world}",
                        "l2": f"inputs {N * F * L / 1e9:.2f} GB per step > L2; no flush"},
             "paths": paths, "kernels": kernels, "roofline": roofline,
@@ -406,6 +422,20 @@ def main() -> None:
         torch.distributed.destroy_process_group()
 
 
+# DRAM bytes per launch of the precision workload's kernels (24 inputs, n_freq
+# 16384) from one ncu capture of 256-frame launches (profiles/*_precision-24in-
+# nf16384.md), scaled by frames: the F-engine's traffic is all per frame; the
+# X-engines' is the spectra read (per frame) plus the row's read and write.
+_NCU_256 = {"fengine": (944.502784e6, 0.0), "xengine": (805.306368e6, 75.464e6)}
+
+
+def ncu_traffic(kernel: str, workload: str, frames: int):
+    if workload != "precision-24in-nf16384":
+        return None
+    per, fixed = _NCU_256["fengine" if kernel == "fengine" else "xengine"]
+    return per * frames / 256 + fixed
+
+
 def run_batching(pkg, synth, torch, xmode, stream) -> dict:
     """64 uneven integration blocks captured in one CUDA graph (corrx_batch_*)."""
     import ctypes as C
@@ -415,6 +445,7 @@ def run_batching(pkg, synth, torch, xmode, stream) -> dict:
     plan = synth.block_plan(w)
     nblk = len(plan)
     eng = pkg.FxEngine(w.n_station, w.n_freq, PASS_FRAMES, xmode=xmode)
+    eng.autotune(stream)
     rows = torch.empty((nblk, w.n_baseline, w.n_freq), dtype=torch.complex64, device="cuda")
     host = torch.empty((nblk, w.n_baseline, w.n_freq), dtype=torch.complex64).pin_memory()
     first = (C.c_int64 * nblk)(*[b[0] for b in plan])
@@ -457,6 +488,7 @@ def run_stream(pkg, synth, torch, stream) -> dict:
     x, mask = synth.generate_torch(w, w.frames)
     eng = pkg.FxEngine(w.n_station, w.n_freq, PASS_FRAMES,
                        xmode=pkg.abi.CORR_X_TC_FP16_SPLIT)
+    tiles = eng.autotune(stream)
     acc = eng.new_acc()
 
     def step():
@@ -478,6 +510,7 @@ def run_stream(pkg, synth, torch, stream) -> dict:
     gs = w.n_station * w.frames * w.fft_len / (ms * 1e-3) / 1e9
     need = w.n_station * 0.25
     return {"workload": w.name, "xengine": "tc_split", "value": gs, "unit": "GSample/s",
+            "tiles": {k: tiles[k] for k in ("ytile", "xct", "xkt")},
             "ms_per_integration": ms, "real_time_factor": gs / need,
             "real_time_need_gsps": need,
             "integrations_per_60s": 60.0 * 250e6 / (w.frames * w.fft_len)}
@@ -490,6 +523,7 @@ def run_e2e(pkg, w, x, mask, xmode, args, torch) -> dict:
     cfg = pkg.make_config(N, w.n_freq, fps, fps, block_slots, 1)
     c = pkg.Correlator(cfg)
     c.set_xengine(xmode)
+    c.autotune()
     # fill the ring once from the device-resident inputs (receive side's job)
     host = x[:, : fps * block_slots].cpu().numpy()
     for g in range(N):
