@@ -88,6 +88,7 @@ struct Context {
     cudaEvent_t row_done = nullptr, fetch_done = nullptr;
 
     uint64_t bytes_h2d = 0, bytes_d2h = 0, transfers = 0;
+    uint64_t chunks_skipped = 0;   // chunks with no valid frame in any station
     Timing timing;
 
     size_t out_bytes() const {
@@ -195,7 +196,29 @@ corr_status expect_copying(Context *c, int32_t slot, int64_t seq) {
     return CORR_OK;
 }
 
-// The chunked copy + F/X sequence of one slot.
+// Does any station mark a frame of [f0, f0 + ft) of this slot valid? The mask
+// bytes sit in host staging memory, written by the receive side before
+// row_accumulate, so they are read here directly.
+bool chunk_has_frames(const Context *c, const uint8_t *mask_base, int f0, int ft) {
+    const Layout &L = c->lay;
+    const int b0 = f0 >> 3, b1 = (f0 + ft - 1) >> 3;
+    const uint8_t lo = static_cast<uint8_t>(0xFFu << (f0 & 7));
+    const uint8_t hi = static_cast<uint8_t>(0xFFu >> (7 - ((f0 + ft - 1) & 7)));
+    for (int s = 0; s < c->cfg.n_station; ++s) {
+        const uint8_t *m = mask_base + static_cast<size_t>(s) * L.station_stride;
+        for (int b = b0; b <= b1; ++b) {
+            uint8_t keep = 0xFF;
+            if (b == b0) keep &= lo;
+            if (b == b1) keep &= hi;
+            if (m[b] & keep) return true;
+        }
+    }
+    return false;
+}
+
+// The chunked copy + F/X sequence of one slot. A chunk in which no station has
+// a valid frame contributes exactly zero to the row (every frame of it would be
+// zero-filled): it is skipped -- no copy, no F-engine, no X-engine.
 corr_status accumulate_slot(Context *c, int32_t slot, int32_t frames) {
     const corr_config &cfg = c->cfg;
     const Layout &L = c->lay;
@@ -207,6 +230,10 @@ corr_status accumulate_slot(Context *c, int32_t slot, int32_t frames) {
     corr_status st = CORR_OK;
     for (int f0 = 0; f0 < frames; f0 += cfg.chunk_frames) {
         const int ft = frames - f0 < cfg.chunk_frames ? frames - f0 : cfg.chunk_frames;
+        if (!chunk_has_frames(c, mask_base, f0, ft)) {
+            ++c->chunks_skipped;
+            continue;
+        }
         const int d = static_cast<int>(c->chunk_seq++ % kRing);
         const size_t width = static_cast<size_t>(ft) * L.frame_stride;
         if ((st = cuda_check(cudaStreamWaitEvent(c->s_copy, c->compute_done[d], 0),

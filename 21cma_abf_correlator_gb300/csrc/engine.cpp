@@ -157,6 +157,8 @@ corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_s
         fa.y = p->d_y;
         fa.y_frames = p->max_frames;
         fa.ytile = p->ytile;
+        fa.y_fmt = spectra_format(p->xmode);
+        fa.y_scale = spectra_scale(p->n_freq);
         fa.err = p->d_err;
         corr_status st = fengine_launch(p->n_freq, p->tw, fa, p->num_sms, stream);
         if (st != CORR_OK) return st;
@@ -164,6 +166,7 @@ corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_s
         xa.y = p->d_y;
         xa.y_frames = p->max_frames;
         xa.ytile = p->ytile;
+        xa.y_fmt = spectra_format(p->xmode);
         xa.n_station = p->n_station;
         xa.n_freq = p->n_freq;
         xa.frames = ft;
@@ -280,6 +283,8 @@ extern "C" corr_status corrx_run_fengine(void *eng, const int8_t *d_samples,
     fa.y = p->d_y;
     fa.y_frames = p->max_frames;
     fa.ytile = p->ytile;
+    fa.y_fmt = spectra_format(p->xmode);
+    fa.y_scale = spectra_scale(p->n_freq);
     fa.err = p->d_err;
     return fengine_launch(p->n_freq, p->tw, fa, p->num_sms, static_cast<cudaStream_t>(stream));
 }
@@ -296,6 +301,7 @@ extern "C" corr_status corrx_run_xengine(void *eng, int32_t frames, void *d_acc,
     xa.y = p->d_y;
     xa.y_frames = p->max_frames;
     xa.ytile = p->ytile;
+    xa.y_fmt = spectra_format(p->xmode);
     xa.n_station = p->n_station;
     xa.n_freq = p->n_freq;
     xa.frames = frames;
@@ -325,6 +331,11 @@ corr_status fxplan_set_tiles(FxPlan *p, int ytile, int xct, int xkt) {
         if (ytile < xct)
             return failf(CORR_ERR_ARG, "ytile=%d is narrower than the tensor tile (%d channels)",
                          ytile, xct);
+        if (ytile != p->n_freq)
+            return failf(CORR_ERR_ARG,
+                         "the tensor X-engines read FP16 spectra written as contiguous rows: "
+                         "ytile must be n_freq=%d",
+                         p->n_freq);
         p->xct = xct;
         p->xkt = xkt;
     }
@@ -345,10 +356,8 @@ corr_status fxplan_autotune(FxPlan *p, cudaStream_t stream, corrx_tiles *out) {
         const bool split = p->xmode == CORR_X_TC_FP16_SPLIT;
         for (int ct = 8; ct >= 2; ct /= 2)
             for (int kt = 16; kt <= 64; kt *= 2)
-                if (xengine_tc_shape_ok(p->n_station, split, ct, kt)) {
+                if (xengine_tc_shape_ok(p->n_station, split, ct, kt))
                     cands.push_back({p->n_freq, ct, kt});
-                    if (ct < p->n_freq) cands.push_back({ct, ct, kt});
-                }
     }
     if (cands.empty()) return fail(CORR_ERR_INTERNAL, "autotune: no candidate tile");
     const int frames = std::min(p->max_frames, 1024);
@@ -403,7 +412,7 @@ corr_status fxplan_autotune(FxPlan *p, cudaStream_t stream, corrx_tiles *out) {
     int f_ytile = -1;
     float f_ms = 0.f;
     for (const Cand &c : cands) {
-        if ((st = fxplan_set_tiles(p, c.ytile, c.ct, c.kt)) != CORR_OK) break;
+        if (fxplan_set_tiles(p, c.ytile, c.ct, c.kt) != CORR_OK) continue;   // not for this form
         if (c.ytile != f_ytile) {   // the F-engine depends on the layout only
             if ((st = timed(run_f, &f_ms)) != CORR_OK) break;
             f_ytile = c.ytile;

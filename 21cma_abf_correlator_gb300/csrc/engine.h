@@ -12,6 +12,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <algorithm>
+#include <cmath>
 #include <string>
 
 #include <cuda_runtime.h>
@@ -66,6 +67,26 @@ __host__ __device__ inline size_t y_index(int c, int f, int s, int n_station, in
            (c % ytile);
 }
 
+/// How the F-engine stores a bin for each X-engine: FP32 pairs (plain); FP16
+/// pairs scaled by spectra_scale (FP16 tensor form); or the split form's operands,
+/// the scaled FP16 pair h then l = fp16(scaled - h), 8 bytes like FP32.
+enum SpectraFormat : int { kSpectraF32 = 0, kSpectraF16 = 1, kSpectraF16Split = 2 };
+
+inline int spectra_format(int xmode) {
+    return xmode == CORR_X_TC_FP16         ? kSpectraF16
+           : xmode == CORR_X_TC_FP16_SPLIT ? kSpectraF16Split
+                                           : kSpectraF32;
+}
+
+/// The power of two that FP16 spectra are scaled by: spectra of int8 frames
+/// satisfy |Y| <= 128*L, so 2^-(log2 L - 8) keeps every bin below 2^15, inside
+/// FP16's range, for every input; products are unscaled by its inverse square.
+inline float spectra_scale(int n_freq) {
+    int l = 0;
+    while ((1 << l) < 2 * n_freq) ++l;
+    return std::ldexp(1.0f, -(l - 8));
+}
+
 /// Arguments of one F-engine launch: `frames` x `n_station` real FFTs.
 struct FengineArgs {
     const int8_t *samples;      // frame f of station s: samples + s*station_stride + f*frame_stride
@@ -79,6 +100,8 @@ struct FengineArgs {
     float2 *y;                  // spectra (y_index)
     int y_frames;               // frames the spectra buffer holds
     int ytile;                  // channels per spectra tile
+    int y_fmt;                  // SpectraFormat of the stored bins (scaled by y_scale if FP16)
+    float y_scale;
     int *err;
 };
 
@@ -87,6 +110,7 @@ struct XengineArgs {
     const float2 *y;            // as FengineArgs::y
     int y_frames;               // frames the spectra buffer holds (>= frames)
     int ytile;                  // channels per spectra tile
+    int y_fmt;                  // SpectraFormat of the bins
     int n_station;
     int n_freq;
     int frames;

@@ -24,7 +24,10 @@
 // writes 32 consecutive bins per warp store: whole pieces of ytile*8 bytes.
 
 #include <cmath>
+#include <type_traits>
 #include <vector>
+
+#include <cuda_fp16.h>
 
 #include "engine.h"
 #include "ptx.cuh"
@@ -186,7 +189,8 @@ struct FeCfg {
     static constexpr int OFF_PHI = OFF_PLO + 64 * 8;
     static constexpr int OFF_QLO = OFF_PHI + N_PASS_HI * 8;
     static constexpr int OFF_QHI = OFF_QLO + 64 * 8;
-    static constexpr int OFF_BAR = (OFF_QHI + N_POST_HI * 8 + 15) / 16 * 16;
+    static constexpr int OFF_T2 = OFF_QHI + N_POST_HI * 8;   // second-pass twiddles
+    static constexpr int OFF_BAR = (OFF_T2 + R0 * R1 * 8 + 15) / 16 * 16;
     static constexpr int OFF_FLAG = OFF_BAR + 16;
     static constexpr int SMEM = OFF_FLAG + 16;
     // CTAs per SM the launch bounds plan for: as many as shared memory allows,
@@ -196,6 +200,17 @@ struct FeCfg {
     static constexpr int MIN_BLOCKS =
         (BY_SMEM < BY_REGS ? BY_SMEM : BY_REGS) < 1 ? 1 : (BY_SMEM < BY_REGS ? BY_SMEM : BY_REGS);
 };
+
+// Two signed bytes (little-endian pair) -> two floats, exactly, without the
+// conversion unit: flipping the sign bit gives b + 128 in [0, 255]; placed in the
+// low byte of 0x4B000000 that is the float 2^23 + b + 128, and subtracting
+// 2^23 + 128 leaves b.
+__device__ __forceinline__ float2 int8_pair_to_float2(uint16_t u) {
+    const uint32_t x = static_cast<uint32_t>(u) ^ 0x8080u;
+    const float lo = __uint_as_float(__byte_perm(x, 0x4B000000u, 0x7440));
+    const float hi = __uint_as_float(__byte_perm(x, 0x4B000000u, 0x7441));
+    return make_float2(lo - 8388736.0f, hi - 8388736.0f);
+}
 
 // Shared-memory index padding: one float2 per R0 elements, which makes the
 // stride-R0 scatter of the first pass conflict-free and keeps every other
@@ -207,9 +222,12 @@ __device__ __forceinline__ int padi(int i) { return i + (i >> SHIFT); }
 //   out[(j/NS)*NS*R + j%NS + r*NS] = DFT_R( in[j + r*M/R] * w^(r*(j%NS)) )
 // Each thread owns P/R butterflies. In place: read all, barrier, write all,
 // barrier. The first pass reads int8 sample pairs instead of shared data.
-template <int M, int T, int P, int R, int NS, int SHIFT, bool FIRST>
+// TAB: the pass's twiddles w^(r*(j%NS)) (NS*R of them) come from table `t2`
+// laid out [r][j%NS] instead of from the two-level tables.
+template <int M, int T, int P, int R, int NS, int SHIFT, bool FIRST, bool TAB = false>
 __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *__restrict__ sx,
-                                         const float2 *lo, const float2 *hi, int tid) {
+                                         const float2 *lo, const float2 *hi, int tid,
+                                         const float2 *t2 = nullptr) {
     constexpr int NB = P / R;
     constexpr int STRIDE = M / R;
     static_assert(NB >= 1 && NB * R == P, "bad radix plan");
@@ -226,16 +244,21 @@ __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *_
         const int j = tid + q * T;
         if constexpr (FIRST) {
 #pragma unroll
-            for (int r = 0; r < R; ++r) {
-                const char2 c = sx[j + r * STRIDE];
-                v[q][r] = make_float2(static_cast<float>(c.x), static_cast<float>(c.y));
-            }
+            for (int r = 0; r < R; ++r)
+                v[q][r] = int8_pair_to_float2(
+                    reinterpret_cast<const uint16_t *>(sx)[j + r * STRIDE]);
         } else {
             const int pj = padi<SHIFT>(j);
 #pragma unroll
             for (int r = 0; r < R; ++r) v[q][r] = sd[pj + r * PSTRIDE];
         }
-        if constexpr (NS > 1) apply_twiddles<R>(v[q], (j & (NS - 1)) * (M / (NS * R)), lo, hi);
+        if constexpr (TAB) {
+            const float2 *tj = t2 + (j & (NS - 1));
+#pragma unroll
+            for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], tj[r * NS]);
+        } else if constexpr (NS > 1) {
+            apply_twiddles<R>(v[q], (j & (NS - 1)) * (M / (NS * R)), lo, hi);
+        }
         Dft<R>::run(v[q]);
     }
     __syncthreads();
@@ -251,27 +274,50 @@ __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *_
 
 // Where bin k of the current (frame, station) goes in the channel-tiled layout.
 // (Element indices fit 32 bits: the spectra buffer holds < 2^32 values.)
+// Bin formats: FP32 pairs; FP16 pairs scaled by `scale` (a power of two, so the
+// scaling is exact), the FP16 tensor X-engine's operands; or the split form's
+// operands, the FP16 pair h = fp16(v*scale) followed by l = fp16(v*scale - h).
+// CONTIG: ytile = n_freq, one contiguous row, bin k at base[k].
+template <int FMT, bool CONTIG>
 struct YRow {
-    float2 *base;          // y + (f*n_station + s)*ytile
+    using T = typename std::conditional<
+        FMT == kSpectraF32, float2,
+        typename std::conditional<FMT == kSpectraF16, __half2, uint2>::type>::type;
+    T *base;               // y + (f*n_station + s)*ytile
     uint32_t tile_stride;  // y_frames*n_station*ytile
     int shift;             // log2(ytile)
-    __device__ __forceinline__ float2 &operator[](int k) const {
-        return base[static_cast<uint32_t>(k >> shift) * tile_stride +
-                    static_cast<uint32_t>(k & ((1 << shift) - 1))];
+    float scale;
+    __device__ __forceinline__ void put(int k, float2 v) const {
+        T *dst = CONTIG ? base + k
+                        : base + (static_cast<uint32_t>(k >> shift) * tile_stride +
+                                  static_cast<uint32_t>(k & ((1 << shift) - 1)));
+        if constexpr (FMT == kSpectraF16) {
+            *dst = __floats2half2_rn(v.x * scale, v.y * scale);
+        } else if constexpr (FMT == kSpectraF16Split) {
+            const float x = v.x * scale, y = v.y * scale;
+            const __half2 h = __floats2half2_rn(x, y);
+            const float2 hf = __half22float2(h);
+            const __half2 l = __floats2half2_rn(x - hf.x, y - hf.y);
+            *dst = make_uint2(*reinterpret_cast<const uint32_t *>(&h),
+                              *reinterpret_cast<const uint32_t *>(&l));
+        } else {
+            *dst = v;
+        }
     }
 };
 
 // X[k] = Fe + w_k Fo and X[M-k] = conj(Fe - w_k Fo), with Z = FFT of the packed
 // pairs, Fe = (Z[k] + conj(Z[M-k]))/2, Fo = -i (Z[k] - conj(Z[M-k]))/2 and
 // w_k = exp(-2*pi*i*k/L) passed in. `both` = false skips X[M-k] (k = 0: Nyquist).
+template <class Row>
 __device__ __forceinline__ void split_store(float2 zk, float2 zmk, float2 w, int k, int M,
-                                            bool both, const YRow &yrow) {
+                                            bool both, const Row &yrow) {
     const float2 zm = make_float2(zmk.x, -zmk.y);
     const float2 fe = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y + zm.y));
     const float2 fo = make_float2(0.5f * (zk.y - zm.y), -0.5f * (zk.x - zm.x));
     const float2 wf = cmul(w, fo);
-    yrow[k] = cadd(fe, wf);
-    if (both) yrow[M - k] = make_float2(fe.x - wf.x, wf.y - fe.y);
+    yrow.put(k, cadd(fe, wf));
+    if (both) yrow.put(M - k, make_float2(fe.x - wf.x, wf.y - fe.y));
 }
 
 // Last pass (radix R2, NS = J) fused with the split and the global store.
@@ -282,11 +328,11 @@ __device__ __forceinline__ void split_store(float2 zk, float2 zmk, float2 w, int
 // warp diverges; only X[M/2] = conj(Z[M/2]) is one extra store for thread 0.
 // Split twiddles: k = j + i*J gives w_k = w_j * exp(-pi*i*i/R2), one table
 // lookup per butterfly times compile-time constants.
-template <int LOGM>
+template <int LOGM, class Row>
 __device__ __forceinline__ void last_pass_store(const float2 *__restrict__ sd,
                                                 const float2 *plo, const float2 *phi,
                                                 const float2 *qlo, const float2 *qhi,
-                                                const YRow &yrow, int tid) {
+                                                const Row &yrow, int tid) {
     using C = FeCfg<LOGM>;
     constexpr int M = C::M, J = C::J, R = C::R2, H = R / 2;
     static_assert(J % (1 << C::PADSHIFT) == 0, "last-pass stride");
@@ -307,26 +353,27 @@ __device__ __forceinline__ void last_pass_store(const float2 *__restrict__ sd,
     Dft<R>::run(b);   // b[r] = Z[j2 + r*J]
     const float2 w1 = cmul(qlo[j1 & 63], qhi[j1 >> 6]);   // w_{j1}
     const float2 w2 = cmul(qlo[j2 & 63], qhi[j2 >> 6]);   // w_{j2} (thread 0: w_{J/2})
+    // Second half (i >= H): thread 0 pairs b with itself from k = J/2; the
+    // others continue k = j1 + i*J. Both as a base index and a base twiddle
+    // chosen once, stepped by compile-time constants.
+    const int kB = t0 ? J / 2 : j1 + H * J;
+    const float2 wB = t0 ? w2 : mul_w32(w1, H * (16 / R));
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-        float2 zk = a[i], zmk = b[R - 1 - i];
-        int k = j1 + i * J;
         // exp(-pi*i*n/R) = exp(-2*pi*i*n*(16/R)/32)
-        float2 w = mul_w32(w1, i * (16 / R));
         if (i < H) {
-            if (t0) {
-                zmk = a[(R - i) % R];
-                k = i * J;
-            }
-        } else if (t0) {
-            zk = b[i - H];
-            zmk = b[R - 1 - (i - H)];
-            k = J / 2 + (i - H) * J;
-            w = mul_w32(w2, (i - H) * (16 / R));
+            // thread 0 (j1 = 0): Z[M - i*J] = Z[(R - i)*J] = a[(R - i) % R]
+            const float2 zmk = t0 ? a[(R - i) % R] : b[R - 1 - i];
+            split_store(a[i], zmk, mul_w32(w1, i * (16 / R)), j1 + i * J, M, !(t0 && i == 0),
+                        yrow);
+        } else {
+            const float2 zk = t0 ? b[i - H] : a[i];
+            const float2 zmk = t0 ? b[R - 1 - (i - H)] : b[R - 1 - i];
+            split_store(zk, zmk, mul_w32(wB, (i - H) * (16 / R)), kB + (i - H) * J, M, true,
+                        yrow);
         }
-        split_store(zk, zmk, w, k, M, !(t0 && i == 0), yrow);
     }
-    if (t0) yrow[M / 2] = make_float2(a[H].x, -a[H].y);
+    if (t0) yrow.put(M / 2, make_float2(a[H].x, -a[H].y));
 }
 
 struct TwPtrs {
@@ -340,7 +387,7 @@ __device__ __forceinline__ bool frame_present(const FengineArgs &a, int f, int s
     return (byte >> (bit & 7)) & 1u;
 }
 
-template <int LOGM>
+template <int LOGM, int FMT, bool CONTIG>
 __global__ void __launch_bounds__(FeCfg<LOGM>::T, FeCfg<LOGM>::MIN_BLOCKS)
     fengine_kernel(FengineArgs a, TwPtrs tw) {
     using C = FeCfg<LOGM>;
@@ -354,6 +401,7 @@ __global__ void __launch_bounds__(FeCfg<LOGM>::T, FeCfg<LOGM>::MIN_BLOCKS)
     float2 *phi = reinterpret_cast<float2 *>(smem + C::OFF_PHI);
     float2 *qlo = reinterpret_cast<float2 *>(smem + C::OFF_QLO);
     float2 *qhi = reinterpret_cast<float2 *>(smem + C::OFF_QHI);
+    float2 *t2 = reinterpret_cast<float2 *>(smem + C::OFF_T2);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + C::OFF_BAR);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + C::OFF_FLAG);
 
@@ -364,6 +412,12 @@ __global__ void __launch_bounds__(FeCfg<LOGM>::T, FeCfg<LOGM>::MIN_BLOCKS)
     }
     for (int i = tid; i < C::N_PASS_HI; i += T) phi[i] = tw.pass_hi[i];
     for (int i = tid; i < C::N_POST_HI; i += T) qhi[i] = tw.post_hi[i];
+    // second pass: t2[r][jj] = exp(-2*pi*i*r*jj/(R0*R1)) = w^u, u = r*jj*M/(R0*R1)
+    for (int i = tid; i < C::R0 * C::R1; i += T) {
+        const int r = i / C::R0, jj = i - r * C::R0;
+        const int u = (r * jj * (M / (C::R0 * C::R1))) & (M - 1);
+        t2[i] = cmul(tw.pass_lo[u & 63], tw.pass_hi[u >> 6]);
+    }
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
@@ -405,35 +459,42 @@ __global__ void __launch_bounds__(FeCfg<LOGM>::T, FeCfg<LOGM>::MIN_BLOCKS)
             bulk_copy_g2s(buf ? sx0 : sx1, src_of(next), frame_bytes, &bar[buf ^ 1]);
             next_issued = true;
         }
-        const YRow yrow{a.y + static_cast<size_t>(item) * a.ytile,
-                        static_cast<uint32_t>(a.y_frames) * a.n_station * a.ytile, ytile_shift};
+        using Row = YRow<FMT, CONTIG>;
+        const Row yrow{
+            reinterpret_cast<typename Row::T *>(a.y) + static_cast<size_t>(item) * a.ytile,
+            static_cast<uint32_t>(a.y_frames) * a.n_station * a.ytile, ytile_shift, a.y_scale};
 
         if (!present(item)) {
             // Missing frame: its samples count as zeros, so does its spectrum.
-            for (int k = tid; k < M; k += T) yrow[k] = make_float2(0.f, 0.f);
+            for (int k = tid; k < M; k += T) yrow.put(k, make_float2(0.f, 0.f));
             continue;
         }
 
+        // Every thread waits for the frame itself: no CTA barrier here, so a
+        // warp that has stored its part of the previous spectrum starts this
+        // item's first pass (which reads only the int8 frame and writes sd after
+        // its own barrier) while other warps are still storing.
         if (!mbar_wait_bounded(&bar[buf], (parity_bits >> buf) & 1u, a.err,
                                kErrFengineCopyTimeout))
             *abort_flag = 1;
-        __syncthreads();
+        parity_bits ^= 1u << buf;
+
+        fft_pass<M, T, C::P, C::R0, 1, C::PADSHIFT, true>(sd, buf ? sx1 : sx0, plo, phi, tid);
+        // the pass ends with a barrier: every thread sees the same flag
         if (*abort_flag) {
             // Let whatever copy is still in flight land before the CTA exits.
             if (tid == 0 && next_issued)
                 mbar_wait_bounded(&bar[buf ^ 1], (parity_bits >> (buf ^ 1)) & 1u, nullptr, 0);
             return;
         }
-        parity_bits ^= 1u << buf;
-
-        fft_pass<M, T, C::P, C::R0, 1, C::PADSHIFT, true>(sd, buf ? sx1 : sx0, plo, phi, tid);
-        fft_pass<M, T, C::P, C::R1, C::R0, C::PADSHIFT, false>(sd, nullptr, plo, phi, tid);
+        fft_pass<M, T, C::P, C::R1, C::R0, C::PADSHIFT, false, true>(sd, nullptr, plo, phi, tid,
+                                                                    t2);
         last_pass_store<LOGM>(sd, plo, phi, qlo, qhi, yrow, tid);
         // The next item's first pass synchronises before it overwrites sd.
     }
 }
 
-template <int LOGM>
+template <int LOGM, int FMT, bool CONTIG>
 corr_status launch_one(const FengineArgs &a, const TwiddleTables &tw, int num_sms,
                        cudaStream_t stream) {
     using C = FeCfg<LOGM>;
@@ -441,13 +502,13 @@ corr_status launch_one(const FengineArgs &a, const TwiddleTables &tw, int num_sm
     static int per_sm = 1;
     if (!configured) {
         corr_status st = cuda_check(
-            cudaFuncSetAttribute(fengine_kernel<LOGM>,
+            cudaFuncSetAttribute(fengine_kernel<LOGM, FMT, CONTIG>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM),
             "cudaFuncSetAttribute(fengine)");
         if (st != CORR_OK) return st;
         int blocks = 0;
         st = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                            &blocks, fengine_kernel<LOGM>, C::T, C::SMEM),
+                            &blocks, fengine_kernel<LOGM, FMT, CONTIG>, C::T, C::SMEM),
                         "cudaOccupancyMaxActiveBlocksPerMultiprocessor(fengine)");
         if (st != CORR_OK) return st;
         if (blocks < 1)
@@ -460,8 +521,22 @@ corr_status launch_one(const FengineArgs &a, const TwiddleTables &tw, int num_sm
     int grid = num_sms * per_sm;
     if (grid > items) grid = items;
     TwPtrs p{tw.pass_lo, tw.pass_hi, tw.post_lo, tw.post_hi};
-    fengine_kernel<LOGM><<<grid, C::T, C::SMEM, stream>>>(a, p);
+    fengine_kernel<LOGM, FMT, CONTIG><<<grid, C::T, C::SMEM, stream>>>(a, p);
     return cuda_check(cudaGetLastError(), "fengine_kernel launch");
+}
+
+template <int LOGM>
+corr_status launch_size(const FengineArgs &a, const TwiddleTables &tw, int num_sms,
+                        cudaStream_t stream) {
+    const bool contig = a.ytile == (1 << LOGM);
+    if (a.y_fmt != kSpectraF32) {
+        if (!contig)
+            return fail(CORR_ERR_ARG, "FP16 spectra are written as contiguous rows (ytile = n_freq)");
+        if (a.y_fmt == kSpectraF16) return launch_one<LOGM, kSpectraF16, true>(a, tw, num_sms, stream);
+        return launch_one<LOGM, kSpectraF16Split, true>(a, tw, num_sms, stream);
+    }
+    if (contig) return launch_one<LOGM, kSpectraF32, true>(a, tw, num_sms, stream);
+    return launch_one<LOGM, kSpectraF32, false>(a, tw, num_sms, stream);
 }
 
 int ilog2(int v) {
@@ -524,12 +599,12 @@ void fengine_release(TwiddleTables *tw) {
 corr_status fengine_launch(int n_freq, const TwiddleTables &tw, const FengineArgs &a,
                            int num_sms, cudaStream_t stream) {
     switch (ilog2(n_freq)) {
-    case 9: return launch_one<9>(a, tw, num_sms, stream);
-    case 10: return launch_one<10>(a, tw, num_sms, stream);
-    case 11: return launch_one<11>(a, tw, num_sms, stream);
-    case 12: return launch_one<12>(a, tw, num_sms, stream);
-    case 13: return launch_one<13>(a, tw, num_sms, stream);
-    case 14: return launch_one<14>(a, tw, num_sms, stream);
+    case 9: return launch_size<9>(a, tw, num_sms, stream);
+    case 10: return launch_size<10>(a, tw, num_sms, stream);
+    case 11: return launch_size<11>(a, tw, num_sms, stream);
+    case 12: return launch_size<12>(a, tw, num_sms, stream);
+    case 13: return launch_size<13>(a, tw, num_sms, stream);
+    case 14: return launch_size<14>(a, tw, num_sms, stream);
     default:
         return failf(CORR_ERR_ARG, "F-engine: n_freq=%d is not a power of two in [512, 16384]",
                      n_freq);

@@ -152,6 +152,8 @@ extern "C" corr_status corrx_accumulate_noalloc(int32_t n_station, int32_t n_fre
     fa.y = d.spectra;
     fa.y_frames = frames;
     fa.ytile = n_freq;
+    fa.y_fmt = spectra_format(xmode);
+    fa.y_scale = spectra_scale(n_freq);
     fa.err = nullptr;
     if ((st = fengine_launch(n_freq, tw, fa, d.num_sms, s)) != CORR_OK) return st;
 
@@ -159,6 +161,7 @@ extern "C" corr_status corrx_accumulate_noalloc(int32_t n_station, int32_t n_fre
     xa.y = d.spectra;
     xa.y_frames = frames;
     xa.ytile = n_freq;
+    xa.y_fmt = spectra_format(xmode);
     xa.n_station = n_station;
     xa.n_freq = n_freq;
     xa.frames = frames;

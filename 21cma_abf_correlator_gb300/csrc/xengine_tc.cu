@@ -9,7 +9,8 @@
 // The tensor cores compute S with K = frames, FP16 operands and FP32 accumulation
 // in tensor memory (TMEM), accumulated over the whole launch.
 //
-// Precision forms:
+// Precision forms (the F-engine stores the spectra already in the form's
+// operand precision, scaled, so the converters here only transpose):
 //   FP16       : D rounded once to FP16 (11-bit significand).
 //   FP16 split : D = Dh + Dl, Dh = fp16(D), Dl = fp16(D - Dh) (about 22 bits);
 //                S ~ H + P + P^T with H = Dh^T Dh and P = Dl^T Dh (Dl^T Dl dropped).
@@ -40,13 +41,14 @@
 //
 // Warp-specialised persistent CTAs, one per SM (TMEM), CT channels per tile:
 //   warp 0 (lane 0): TMA tensor loads -- one 4-D box {CT channels, N stations,
-//     KT frames, 1 tile} of the spectra per stage (3-D, KT rows of CT*N, when
-//     the spectra tiles are CT wide) into a ring as deep as shared memory allows.
+//     KT frames, 1 tile} of the spectra per stage into a ring as deep as shared
+//     memory allows.
 //     The map ends at the launch's last frame, so a partial stage arrives
 //     zero-padded.
 //   warp 1 (lane 0): the MMAs of a stage once its operands are written.
-//   warps 2-9 (converters): scale, round and split a landed stage into the
-//     K-major no-swizzle operand layout (8-row x 16-byte core matrices).
+//   warps 2-9 (converters): regroup a landed stage (FP16 bins, frame-major)
+//     into the K-major no-swizzle operand layout (8-row x 16-byte core
+//     matrices, frames along K) with byte permutes.
 //   warps 10-13 (epilogue, one per TMEM lane quarter): after a tile's last MMA,
 //     read the accumulators (tcgen05.ld), pair rows 2j/2j+1 with one shuffle,
 //     stage V (and Q), release TMEM, then add V into the row in global memory
@@ -93,7 +95,8 @@ struct TcGeom {
     int acc_cols;      // TMEM columns of one accumulator set (a tile)
     int n_acc;         // accumulator sets (2 = the next tile's MMAs overlap the epilogue)
     int op_stage;      // operand bytes per stage
-    int ld_stage;      // fp32 bytes per stage = kt * N * ct * 8
+    int elem;          // bytes per spectrum bin: 8 (FP32 pairs) or 4 (FP16 pairs)
+    int ld_stage;      // spectra bytes per stage = kt * N * ct * elem
     int n_ld;
     int n_op;
     int vs_bytes;      // staged V: ct planes of n_baseline float2, k-major triangle
@@ -122,6 +125,11 @@ TcGeom make_geom(int n_station, bool split, int ct, int kt) {
     if (N < 1 || N > 64 || (kt != 16 && kt != 32 && kt != 64) || ct < 2 || ct > 8 ||
         (ct & (ct - 1)))
         return g;
+    // Both forms read FP16 spectra written so by the F-engine: pairs (4 bytes)
+    // or hi/lo pairs (8 bytes); a TMA box row of CT of them must be a multiple
+    // of 16 bytes.
+    g.elem = split ? 8 : 4;
+    if (ct * g.elem < 16) return g;
     g.R = round_up(2 * N, 8);
     int rows_valid;
     if (split) {
@@ -160,7 +168,7 @@ TcGeom make_geom(int n_station, bool split, int ct, int kt) {
     const int reach = std::max(16, g.nb / 8) * g.sbo;
     const int slack = std::max(0, reach - g.region_stride) + 7 * 16 + 128;
     g.op_stage = round_up(g.regions * g.region_stride + slack, 128);
-    g.ld_stage = kt * N * ct * 8;
+    g.ld_stage = kt * N * ct * g.elem;
     g.items = ct * N * (kt / 8);
     if (g.items > kMaxItems * kConverters) return g;
     const int n_baseline = N * (N + 1) / 2;
@@ -250,30 +258,15 @@ __device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, i
         : "memory");
 }
 
-// 3-D TMA tile load global -> shared, completing on `bar`.
-__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z,
-                                            uint64_t *bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
-        "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
-        : "memory");
-}
-
-__device__ __forceinline__ uint32_t half2_bits(__half2 h) {
-    return *reinterpret_cast<const uint32_t *>(&h);
-}
-
 struct TcParams {
     int ytile;
-    int merged;        // ytile == ct: the map is (ct*N, frame, tile), one row per frame
+    int in_fmt;        // SpectraFormat: FP16 pairs, or FP16 hi/lo pairs (already scaled)
     int n_station;
     int n_freq;
     int frames;
     float2 *acc;
     int *err;
-    float scale;       // power of two applied before rounding to fp16
-    float inv_scale2;  // 1/scale^2
+    float inv_scale2;  // 1/scale^2: undoes the F-engine's spectra scale in S
     TcGeom g;
 };
 
@@ -383,12 +376,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const int c0 = tile_c0(tl);
                 mbar_arrive_expect_tx(&bars.load_full[slot], static_cast<uint32_t>(g.ld_stage));
                 // frames past `frames` (the map's last frame) arrive as zeros
-                if (p.merged)
-                    tma_load_3d(ld_ring + slot * g.ld_stage, &ymap, 0, st * g.kt, c0 / p.ytile,
-                                &bars.load_full[slot]);
-                else
-                    tma_load_4d(ld_ring + slot * g.ld_stage, &ymap, c0 & (p.ytile - 1), 0,
-                                st * g.kt, c0 / p.ytile, &bars.load_full[slot]);
+                tma_load_4d(ld_ring + slot * g.ld_stage, &ymap, c0 & (p.ytile - 1), 0,
+                            st * g.kt, c0 / p.ytile, &bars.load_full[slot]);
                 ++s_ld_issued;
             }
         }
@@ -483,43 +472,59 @@ __global__ void __launch_bounds__(kThreads, 1)
                 s_abort = 1;
                 break;
             }
-            // fp32 slot: [frame][station][CT channels]
+            // spectra slot: [frame][station][CT channels]
             const float2 *ld = reinterpret_cast<const float2 *>(ld_ring + lb * g.ld_stage);
             unsigned char *op = op_ring + ob * g.op_stage;
+            if (p.in_fmt == kSpectraF16) {
+                // FP16 pairs (re, im) per frame: regroup into 8-frame rows of re
+                // and of im, two byte-permutes per frame pair
+                const uint32_t *ld16 = reinterpret_cast<const uint32_t *>(ld);
 #pragma unroll
-            for (int it = 0; it < kMaxItems; ++it) {
-                if (it >= n_item) break;
-                const float2 *src = ld + it_ld[it];
-                uint32_t hre[4], him[4], lre[4], lim[4];
+                for (int it = 0; it < kMaxItems; ++it) {
+                    if (it >= n_item) break;
+                    const uint32_t *src = ld16 + it_ld[it];
+                    uint32_t hre[4], him[4];
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    // frames past `frames` arrived as zeros (the tensor map ends there)
-                    const float2 va = src[(2 * i) * row_step];
-                    const float2 vb = src[(2 * i + 1) * row_step];
-                    const float a0 = va.x * p.scale, a1 = vb.x * p.scale;
-                    const float b0 = va.y * p.scale, b1 = vb.y * p.scale;
-                    const __half2 hr = __floats2half2_rn(a0, a1);
-                    const __half2 hi = __floats2half2_rn(b0, b1);
-                    hre[i] = half2_bits(hr);
-                    him[i] = half2_bits(hi);
-                    if (g.split) {
-                        const float2 fr = __half22float2(hr);
-                        const float2 fi = __half22float2(hi);
-                        lre[i] = half2_bits(__floats2half2_rn(a0 - fr.x, a1 - fr.y));
-                        lim[i] = half2_bits(__floats2half2_rn(b0 - fi.x, b1 - fi.y));
+                    for (int i = 0; i < 4; ++i) {
+                        const uint32_t w0 = src[(2 * i) * row_step];
+                        const uint32_t w1 = src[(2 * i + 1) * row_step];
+                        hre[i] = __byte_perm(w0, w1, 0x5410);
+                        him[i] = __byte_perm(w0, w1, 0x7632);
                     }
+                    unsigned char *dst = op + it_op[it];
+                    *reinterpret_cast<uint4 *>(dst) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
+                    *reinterpret_cast<uint4 *>(dst + 16) =
+                        make_uint4(him[0], him[1], him[2], him[3]);
                 }
-                unsigned char *dst = op + it_op[it];
-                *reinterpret_cast<uint4 *>(dst) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
-                *reinterpret_cast<uint4 *>(dst + 16) = make_uint4(him[0], him[1], him[2], him[3]);
-                if (g.split) {
+            } else {
+                // FP16 hi/lo pairs per frame: the Dh rows from the h words, the Dl
+                // rows from the l words
+                const uint2 *ld2 = reinterpret_cast<const uint2 *>(ld);
+#pragma unroll
+                for (int it = 0; it < kMaxItems; ++it) {
+                    if (it >= n_item) break;
+                    const uint2 *src = ld2 + it_ld[it];
+                    uint32_t hre[4], him[4], lre[4], lim[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const uint2 w0 = src[(2 * i) * row_step];
+                        const uint2 w1 = src[(2 * i + 1) * row_step];
+                        hre[i] = __byte_perm(w0.x, w1.x, 0x5410);
+                        him[i] = __byte_perm(w0.x, w1.x, 0x7632);
+                        lre[i] = __byte_perm(w0.y, w1.y, 0x5410);
+                        lim[i] = __byte_perm(w0.y, w1.y, 0x7632);
+                    }
+                    unsigned char *dst = op + it_op[it];
+                    *reinterpret_cast<uint4 *>(dst) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
+                    *reinterpret_cast<uint4 *>(dst + 16) =
+                        make_uint4(him[0], him[1], him[2], him[3]);
                     *reinterpret_cast<uint4 *>(dst + lo_off) =
                         make_uint4(lre[0], lre[1], lre[2], lre[3]);
                     *reinterpret_cast<uint4 *>(dst + lo_off + 16) =
                         make_uint4(lim[0], lim[1], lim[2], lim[3]);
                 }
             }
-            mbar_arrive(&bars.load_empty[lb]);   // the fp32 slot may be refilled
+            mbar_arrive(&bars.load_empty[lb]);   // the spectra slot may be refilled
             fence_proxy_async_smem();   // operand stores -> visible to the tensor cores
             mbar_arrive(&bars.op_full[ob]);
         }
@@ -671,12 +676,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
 }
 
-int ilog2(int v) {
-    int l = 0;
-    while ((1 << l) < v) ++l;
-    return l;
-}
-
 // cuTensorMapEncodeTiled from the driver, looked up once through the runtime
 // (no link-time dependency on libcuda).
 using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
@@ -737,41 +736,33 @@ corr_status xengine_tc_launch(const XengineArgs &a, bool split, int ct, int kt, 
                      a.ytile, g.ct);
     if ((reinterpret_cast<uintptr_t>(a.acc) & 15) != 0)
         return fail(CORR_ERR_ARG, "the tensor X-engine needs a 16-byte aligned accumulator");
+    if (a.y_fmt != (split ? kSpectraF16Split : kSpectraF16))
+        return fail(CORR_ERR_INTERNAL, "spectra format does not match the X-engine form");
+    if ((a.ytile * g.elem) % 16 != 0)
+        return failf(CORR_ERR_ARG, "spectra tiles of %d bins are not a multiple of 16 bytes",
+                     a.ytile);
     EncodeTiledFn enc = encode_tiled();
     if (enc == nullptr)
         return fail(CORR_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-    // Spectra as 8-byte elements, innermost first. Tiles as wide as the tensor
-    // tile: (channel*station, frame, tile) -- a stage is KT rows of CT*N
-    // contiguous elements. Wider tiles (contiguous rows when ytile = n_freq):
-    // (channel within tile, station, frame, tile), KT*N rows of CT elements.
+    // Spectra as a 4-D array of bins (4 or 8 bytes), innermost first:
+    // (channel within its tile, station, frame, tile); a stage is KT*N rows of
+    // CT bins. The frame extent is the launch's, so frames past it read as zeros.
     CUtensorMap map;
-    const bool merged = a.ytile == g.ct && g.ct * a.n_station <= 256;
-    const cuuint64_t row = static_cast<cuuint64_t>(a.ytile) * 8;
+    const cuuint64_t row = static_cast<cuuint64_t>(a.ytile) * g.elem;
+    const CUtensorMapDataType etype =
+        g.elem == 8 ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32;
     const cuuint32_t estr[4] = {1, 1, 1, 1};
-    CUresult cr;
-    if (merged) {
-        const cuuint64_t dims[3] = {static_cast<cuuint64_t>(a.ytile) * a.n_station,
-                                    static_cast<cuuint64_t>(a.frames),
-                                    static_cast<cuuint64_t>(a.n_freq / a.ytile)};
-        const cuuint64_t strides[2] = {row * a.n_station, row * a.n_station * a.y_frames};
-        const cuuint32_t box[3] = {static_cast<cuuint32_t>(g.ct * a.n_station),
-                                   static_cast<cuuint32_t>(g.kt), 1};
-        cr = enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<float2 *>(a.y), dims, strides,
-                 box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    } else {
-        const cuuint64_t dims[4] = {static_cast<cuuint64_t>(a.ytile),
-                                    static_cast<cuuint64_t>(a.n_station),
-                                    static_cast<cuuint64_t>(a.frames),
-                                    static_cast<cuuint64_t>(a.n_freq / a.ytile)};
-        const cuuint64_t strides[3] = {row, row * a.n_station, row * a.n_station * a.y_frames};
-        const cuuint32_t box[4] = {static_cast<cuuint32_t>(g.ct),
-                                   static_cast<cuuint32_t>(a.n_station),
-                                   static_cast<cuuint32_t>(g.kt), 1};
-        cr = enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, const_cast<float2 *>(a.y), dims, strides,
-                 box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    }
+    const cuuint64_t dims[4] = {static_cast<cuuint64_t>(a.ytile),
+                                static_cast<cuuint64_t>(a.n_station),
+                                static_cast<cuuint64_t>(a.frames),
+                                static_cast<cuuint64_t>(a.n_freq / a.ytile)};
+    const cuuint64_t strides[3] = {row, row * a.n_station, row * a.n_station * a.y_frames};
+    const cuuint32_t box[4] = {static_cast<cuuint32_t>(g.ct), static_cast<cuuint32_t>(a.n_station),
+                               static_cast<cuuint32_t>(g.kt), 1};
+    const CUresult cr =
+        enc(&map, etype, 4, const_cast<float2 *>(a.y), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (cr != CUDA_SUCCESS)
         return failf(CORR_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", static_cast<int>(cr));
     static int configured_smem = 0;
@@ -785,15 +776,14 @@ corr_status xengine_tc_launch(const XengineArgs &a, bool split, int ct, int kt, 
     }
     TcParams p{};
     p.ytile = a.ytile;
-    p.merged = merged ? 1 : 0;
+    p.in_fmt = a.y_fmt;
     p.n_station = a.n_station;
     p.n_freq = a.n_freq;
     p.frames = a.frames;
     p.acc = a.acc;
     p.err = a.err;
-    const int shift = ilog2(2 * a.n_freq) - 8;   // |Y| <= 128*L -> |Y*2^-shift| <= 2^15
-    p.scale = ldexpf(1.0f, -shift);
-    p.inv_scale2 = ldexpf(1.0f, 2 * shift);
+    const float scale = spectra_scale(a.n_freq);   // applied by the F-engine
+    p.inv_scale2 = 1.0f / (scale * scale);
     p.g = g;
     const int n_tiles = a.n_freq / g.ct;
     const int grid = std::min(n_tiles, std::max(1, num_sms));

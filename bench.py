@@ -249,7 +249,8 @@ def main() -> None:
     # plain and split 1e-5 / 2e-5 at any length; FP16 6e-3/sqrt(frames)
     err_bound = {"plain": 1e-5, "tc_split": 2e-5, "tc": 6e-3 / math.sqrt(F)}
 
-    x, mask = synth.generate_torch(w, F, seed_offset=rank)
+    x, mask = synth.generate_torch(
+        w, F, seed_offset=importlib.import_module(PKG_NAME + ".replicas").replica_seed_offset(rank))
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
     samples_step = N * F * L
@@ -314,11 +315,9 @@ def main() -> None:
     clocks = sampler.stop()
     eng.check()
 
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = samples_step * world / (ms * 1e-3) / 1e9
+    replicas = importlib.import_module(PKG_NAME + ".replicas")
+    ms = replicas.slowest_ms(ms, world, device="cuda")
+    value = replicas.job_gsps(samples_step, world, ms)
 
     paths = {}
     for name, (e_, a_, s_) in engines.items():
@@ -358,8 +357,9 @@ def main() -> None:
     t_f /= reps
     t_x /= reps
     mb = synth.mask_bytes(F) if mask is not None else 0
-    f_bytes = N * PASS_FRAMES * L + N * PASS_FRAMES * nf * 8 + (N * mb * PASS_FRAMES // F)
-    x_bytes = N * PASS_FRAMES * nf * 8 + 2 * B * nf * 8
+    elem = 4 if best == "tc" else 8   # bytes per spectrum bin between the engines
+    f_bytes = N * PASS_FRAMES * L + N * PASS_FRAMES * nf * elem + (N * mb * PASS_FRAMES // F)
+    x_bytes = N * PASS_FRAMES * nf * elem + 2 * B * nf * 8
     kernels = {
         "fengine": {"ms_per_launch": t_f, "alg_bytes": f_bytes,
                     "achieved_gbs": f_bytes / (t_f * 1e-3) / 1e9},
@@ -372,7 +372,7 @@ def main() -> None:
     roofline = {"kernel": dom, "bound": "hbm", "achieved": dk["achieved_gbs"],
                 "peak": hbm_peak, "unit": "GB/s", "frac": dk["achieved_gbs"] / hbm_peak,
                 "peak_kind": peak_kind,
-                "traffic": ncu_traffic(dom, w.name, PASS_FRAMES),
+                "traffic": ncu_traffic(dom, w.name, PASS_FRAMES, elem),
                 "alg_bytes_per_launch": dk["alg_bytes"], "frames_per_launch": PASS_FRAMES}
 
     e2e = None
@@ -424,15 +424,17 @@ def main() -> None:
 
 # DRAM bytes per launch of the precision workload's kernels (24 inputs, n_freq
 # 16384) from one ncu capture of 256-frame launches (profiles/*_precision-24in-
-# nf16384.md), scaled by frames: the F-engine's traffic is all per frame; the
-# X-engines' is the spectra read (per frame) plus the row's read and write.
-_NCU_256 = {"fengine": (944.502784e6, 0.0), "xengine": (805.306368e6, 75.464e6)}
+# nf16384.md), scaled by frames: the F-engine reads the int8 frames and writes
+# the spectra; the X-engines read the spectra and read and write the row.
+_NCU_256 = {"fengine": {8: (944.502784e6, 0.0)},
+            "xengine": {8: (805.306368e6, 75.464e6)}}
 
 
-def ncu_traffic(kernel: str, workload: str, frames: int):
-    if workload != "precision-24in-nf16384":
+def ncu_traffic(kernel: str, workload: str, frames: int, elem: int):
+    entry = _NCU_256["fengine" if kernel == "fengine" else "xengine"].get(elem)
+    if workload != "precision-24in-nf16384" or entry is None:
         return None
-    per, fixed = _NCU_256["fengine" if kernel == "fengine" else "xengine"]
+    per, fixed = entry
     return per * frames / 256 + fixed
 
 

@@ -34,7 +34,7 @@ def noalloc(pkg, torch, xmode, x, frames, acc, mask=None, mask_bit0=0):
     return st
 
 
-@pytest.mark.parametrize("xmode", [0, 2])
+@pytest.mark.parametrize("xmode", [0, 1, 2])
 def test_two_calls_match_allocating_entry_point(pkg, cuda, oracle, xmode):
     torch = cuda
     n, nf, frames = 24, 16384, 20          # 20 <= 21 frames the 64 MiB array holds here
@@ -55,8 +55,11 @@ def test_two_calls_match_allocating_entry_point(pkg, cuda, oracle, xmode):
         torch.cuda.synchronize()
         eng.check()
         g, w = got.cpu().numpy(), want.cpu().numpy()
-        assert oracle.rel_rms(g, w) < REL_RMS_TOL
-        assert oracle.rel_rms(g, oracle.correlate(x_np, present)) < REL_RMS_TOL
+        # same kernels, same tiles, one pass each: the same bits
+        assert np.array_equal(g, w)
+        # FP16 spectra: one rounding to 11 bits, errors falling as 1/sqrt(frames)
+        tol = REL_RMS_TOL if xmode != 1 else 1.5e-3 / np.sqrt(frames)
+        assert oracle.rel_rms(g, oracle.correlate(x_np, present)) < tol
     eng.close()
 
 
