@@ -614,29 +614,48 @@ __global__ void __launch_bounds__(kThreads, 1)
             // V (+ Q[j][k] + conj(Q[k][j])) into the row: this CTA is the only
             // writer of these channels in this launch.
             const int c0 = tile_c0(tl);
-            for (int q = et; q < n_baseline * nq; q += kEpilogue) {
-                const int b = q / nq;
-                const int c = (q - b * nq) * 2;
-                const int j = jk[b] >> 8, k = jk[b] & 0xff;
-                const int tri = k * (k + 1) / 2 + j;
-                float2 v0 = Vs[c * plane_v + tri], v1 = Vs[(c + 1) * plane_v + tri];
-                if (g.split) {
-                    const float2 qa0 = Qs[(c * N + k) * N + j], qb0 = Qs[(c * N + j) * N + k];
-                    const float2 qa1 = Qs[((c + 1) * N + k) * N + j];
-                    const float2 qb1 = Qs[((c + 1) * N + j) * N + k];
-                    v0.x += qa0.x + qb0.x;
-                    v0.y += qa0.y - qb0.y;
-                    v1.x += qa1.x + qb1.x;
-                    v1.y += qa1.y - qb1.y;
+            // Four read-modify-writes per thread in flight: all loads first.
+            constexpr int kBatch = 4;
+            const int n_items = n_baseline * nq;
+            for (int q0 = et; q0 < n_items; q0 += kEpilogue * kBatch) {
+                float4 a[kBatch];
+                float4 *dst[kBatch];
+#pragma unroll
+                for (int u = 0; u < kBatch; ++u) {
+                    const int q = q0 + u * kEpilogue;
+                    dst[u] = nullptr;
+                    if (q < n_items) {
+                        const int b = q / nq;
+                        const int c = (q - b * nq) * 2;
+                        dst[u] = reinterpret_cast<float4 *>(p.acc + static_cast<size_t>(b) * p.n_freq +
+                                                            c0 + c);
+                        a[u] = *dst[u];
+                    }
                 }
-                float4 *dst =
-                    reinterpret_cast<float4 *>(p.acc + static_cast<size_t>(b) * p.n_freq + c0 + c);
-                float4 a = *dst;
-                a.x += v0.x;
-                a.y += v0.y;
-                a.z += v1.x;
-                a.w += v1.y;
-                *dst = a;
+#pragma unroll
+                for (int u = 0; u < kBatch; ++u) {
+                    const int q = q0 + u * kEpilogue;
+                    if (q >= n_items) break;
+                    const int b = q / nq;
+                    const int c = (q - b * nq) * 2;
+                    const int j = jk[b] >> 8, k = jk[b] & 0xff;
+                    const int tri = k * (k + 1) / 2 + j;
+                    float2 v0 = Vs[c * plane_v + tri], v1 = Vs[(c + 1) * plane_v + tri];
+                    if (g.split) {
+                        const float2 qa0 = Qs[(c * N + k) * N + j], qb0 = Qs[(c * N + j) * N + k];
+                        const float2 qa1 = Qs[((c + 1) * N + k) * N + j];
+                        const float2 qb1 = Qs[((c + 1) * N + j) * N + k];
+                        v0.x += qa0.x + qb0.x;
+                        v0.y += qa0.y - qb0.y;
+                        v1.x += qa1.x + qb1.x;
+                        v1.y += qa1.y - qb1.y;
+                    }
+                    a[u].x += v0.x;
+                    a[u].y += v0.y;
+                    a[u].z += v1.x;
+                    a[u].w += v1.y;
+                    *dst[u] = a[u];
+                }
             }
             // everyone done with Vs/Qs before the next tile overwrites them
             mbar_arrive(&bars.epi);

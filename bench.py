@@ -42,7 +42,7 @@ REPO = Path(__file__).resolve().parent
 sys.path.insert(0, str(REPO))
 PKG_NAME = "21cma_abf_correlator_gb300"
 METRIC = "fused F+X GSample/s"
-PASS_FRAMES = 512         # default frames per F/X pass on the device-resident path
+PASS_FRAMES = 1024        # default frames per F/X pass on the device-resident path
 
 
 def peaks():
@@ -372,7 +372,9 @@ def main() -> None:
     roofline = {"kernel": dom, "bound": "hbm", "achieved": dk["achieved_gbs"],
                 "peak": hbm_peak, "unit": "GB/s", "frac": dk["achieved_gbs"] / hbm_peak,
                 "peak_kind": peak_kind,
-                "traffic": ncu_traffic(dom, w.name, PASS_FRAMES, elem),
+                "traffic": ncu_traffic(dom, w.name, PASS_FRAMES, best),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a "
+                                  "256-frame launch, scaled to frames_per_launch",
                 "alg_bytes_per_launch": dk["alg_bytes"], "frames_per_launch": PASS_FRAMES}
 
     e2e = None
@@ -423,15 +425,20 @@ def main() -> None:
 
 
 # DRAM bytes per launch of the precision workload's kernels (24 inputs, n_freq
-# 16384) from one ncu capture of 256-frame launches (profiles/*_precision-24in-
-# nf16384.md), scaled by frames: the F-engine reads the int8 frames and writes
-# the spectra; the X-engines read the spectra and read and write the row.
-_NCU_256 = {"fengine": {8: (944.502784e6, 0.0)},
-            "xengine": {8: (805.306368e6, 75.464e6)}}
+# 16384), per X-engine path, from one ncu capture of 256-frame launches
+# (profiles/*_precision-24in-nf16384.md), scaled by frames: the F-engine's
+# traffic is all per frame (int8 read, spectra write); the X-engines' is the
+# spectra read (per frame) plus the row's read and write (per launch).
+_NCU_256 = {
+    "fengine": {"tc": (543.655168e6, 0.0), "tc_split": (944.579584e6, 0.0),
+                "plain": (945.517056e6, 0.0)},
+    "xengine": {"tc": (402.653184e6, 69.501e6), "tc_split": (805.306368e6, 75.578e6),
+                "plain": (805.306368e6, 73.406e6)},
+}
 
 
-def ncu_traffic(kernel: str, workload: str, frames: int, elem: int):
-    entry = _NCU_256["fengine" if kernel == "fengine" else "xengine"].get(elem)
+def ncu_traffic(kernel: str, workload: str, frames: int, path: str):
+    entry = _NCU_256["fengine" if kernel == "fengine" else "xengine"].get(path)
     if workload != "precision-24in-nf16384" or entry is None:
         return None
     per, fixed = entry
