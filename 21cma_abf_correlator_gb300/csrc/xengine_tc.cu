@@ -45,11 +45,12 @@
 //     memory allows.
 //     The map ends at the launch's last frame, so a partial stage arrives
 //     zero-padded.
-//   warp 1 (lane 0): the MMAs of a stage once its operands are written.
-//   warps 2-9 (converters): regroup a landed stage (FP16 bins, frame-major)
-//     into the K-major no-swizzle operand layout (8-row x 16-byte core
-//     matrices, frames along K) with byte permutes.
-//   warps 10-13 (epilogue, one per TMEM lane quarter): after a tile's last MMA,
+//   warps 1..kIssuers (lane 0): the MMAs of a stage once its operands are
+//     written, the operand regions dealt round robin over the issuers.
+//   converter warps: regroup a landed stage (FP16 bins, frame-major) into the
+//     K-major no-swizzle operand layout (8-row x 16-byte core matrices, frames
+//     along K) with byte permutes.
+//   last four warps (epilogue, one per TMEM lane quarter): after a tile's last MMA,
 //     read the accumulators (tcgen05.ld), pair rows 2j/2j+1 with one shuffle,
 //     stage V (and Q), release TMEM, then add V into the row in global memory
 //     with 16-byte read-modify-writes (one owner per channel tile and launch).
@@ -68,11 +69,18 @@
 namespace corrgb {
 namespace {
 
-constexpr int kConverters = 256;                 // warps 2-9
-constexpr int kEpilogue = 128;                   // warps 10-13
-constexpr int kThreads = 64 + kConverters + kEpilogue;
-constexpr int kFirstConverterWarp = 2;
+// Warp layout (512 threads): warp 0 TMA; warps 1..kIssuers MMA issue (one
+// thread each, operand regions dealt round robin: the issue of tcgen05.mma
+// costs the issuing thread more than the tensor cores need per small MMA, so
+// independent accumulators are issued from several threads); then converter
+// warps; the last four warps are the epilogue (one per TMEM lane quarter).
+constexpr int kIssuers = 4;
+constexpr int kThreads = 512;
+constexpr int kEpilogue = 128;
+constexpr int kFirstConverterWarp = 1 + kIssuers;
+constexpr int kConverters = kThreads - kEpilogue - 32 * kFirstConverterWarp;
 constexpr int kFirstEpilogueWarp = kFirstConverterWarp + kConverters / 32;
+static_assert(kConverters >= 192 && kFirstEpilogueWarp * 32 + kEpilogue == kThreads, "layout");
 constexpr int kMaxLoadStages = 6;
 constexpr int kMaxOpStages = 3;
 constexpr int kMaxItems = 4;                     // conversion items per converter thread
@@ -328,14 +336,14 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         for (int s = 0; s < g.n_op; ++s) {
             mbar_init(&bars.op_full[s], kConverters);
-            mbar_init(&bars.op_empty[s], 1);
+            mbar_init(&bars.op_empty[s], kIssuers);
         }
         for (int s = 0; s < 2; ++s) {
-            mbar_init(&bars.acc_full[s], 1);
+            mbar_init(&bars.acc_full[s], kIssuers);
             mbar_init(&bars.acc_empty[s], kEpilogue);
         }
         mbar_init(&bars.epi, kEpilogue);
-        mbar_init(&bars.fin, 1);
+        mbar_init(&bars.fin, kIssuers);
         s_abort = 0;
         s_ld_issued = 0;
         fence_mbar_init();
@@ -381,18 +389,18 @@ __global__ void __launch_bounds__(kThreads, 1)
                 ++s_ld_issued;
             }
         }
-    } else if (warp == 1) {
+    } else if (warp < kFirstConverterWarp) {
         // ------------------------------ MMAs ------------------------------
+        // issuer i: regions i, i + kIssuers, ... Every issuer commits every
+        // stage (op_empty and acc_full count kIssuers arrivals), with or
+        // without MMAs of its own.
+        const int issuer = warp - 1;
         if (lane == 0) {
             const uint32_t idesc = instr_desc_f16_f32(128, g.nb);
             const int ksteps = g.kt / 16;
             // Descriptors differ only in their start-address field, which
             // cannot carry: (address >> 4) of shared memory fits its 14 bits.
             const uint64_t desc0 = smem_desc(smem_addr(op_ring), g.sbo);
-            uint32_t roff[8];
-#pragma unroll
-            for (int r = 0; r < 8; ++r)
-                roff[r] = static_cast<uint32_t>(r * g.region_stride + region_skew(r)) >> 4;
             for (int gs = 0; gs < total && *abort_flag == 0; ++gs) {
                 const int tl = gs / n_stages;
                 const int st = gs - tl * n_stages;
@@ -415,11 +423,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                 tc_fence_after();
                 const uint64_t dstage = desc0 + (static_cast<uint32_t>(ob * g.op_stage) >> 4);
                 const uint32_t dset = tmem + static_cast<uint32_t>(aset * g.acc_cols);
-#pragma unroll
-                for (int r = 0; r < 8; ++r) {
-                    if (r >= g.regions) break;
+                for (int r = issuer; r < g.regions; r += kIssuers) {
                     const uint32_t d = dset + static_cast<uint32_t>(r * g.nb);
-                    const uint64_t dr = dstage + roff[r];
+                    const uint64_t dr =
+                        dstage + (static_cast<uint32_t>(r * g.region_stride + region_skew(r)) >> 4);
                     for (int ks = 0; ks < ksteps; ++ks) {
                         const uint64_t desc = dr + static_cast<uint32_t>(ks * 2 * kLBO / 16);
                         umma_f16(d, desc, desc, idesc, (st > 0 || ks > 0) ? 1u : 0u);
@@ -668,10 +675,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     tc_fence_before();
     __syncthreads();
-    if (s_abort && tid == 32) {
+    if (s_abort && warp >= 1 && warp < kFirstConverterWarp && lane == 0) {
         // Let every MMA this CTA issued finish before TMEM goes away (bounded;
         // the watchdog code is already recorded). A commit covers the issuing
-        // thread's earlier MMAs.
+        // thread's earlier MMAs; fin completes once every issuer committed.
         umma_commit(&bars.fin);
         mbar_wait_bounded(&bars.fin, 0u, nullptr, 0);
     }
