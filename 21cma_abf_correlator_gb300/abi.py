@@ -107,6 +107,7 @@ class corrx_tiles(C.Structure):
         ("ytile", C.c_int32),
         ("xct", C.c_int32),
         ("xkt", C.c_int32),
+        ("fplan", C.c_int32),
         ("ms_fengine", C.c_float),
         ("ms_xengine", C.c_float),
     ]

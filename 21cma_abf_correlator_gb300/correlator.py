@@ -142,7 +142,7 @@ class Correlator:
         """Pick the fastest spectra layout and tensor X tile for this context's engine."""
         t = abi.corrx_tiles(struct_size=C.sizeof(abi.corrx_tiles))
         abi.check(self.lib.corr_autotune(self.ctx, C.byref(t)), "corr_autotune")
-        return {"ytile": t.ytile, "xct": t.xct, "xkt": t.xkt,
+        return {"ytile": t.ytile, "xct": t.xct, "xkt": t.xkt, "fplan": t.fplan,
                 "ms_fengine": t.ms_fengine, "ms_xengine": t.ms_xengine}
 
     def stats(self) -> abi.corr_device_stats:

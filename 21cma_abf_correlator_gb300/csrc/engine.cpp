@@ -158,6 +158,7 @@ corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_s
         fa.y_frames = p->max_frames;
         fa.ytile = p->ytile;
         fa.y_fmt = spectra_format(p->xmode);
+        fa.fplan = p->fplan;
         fa.y_scale = spectra_scale(p->n_freq);
         fa.err = p->d_err;
         corr_status st = fengine_launch(p->n_freq, p->tw, fa, p->num_sms, stream);
@@ -284,6 +285,7 @@ extern "C" corr_status corrx_run_fengine(void *eng, const int8_t *d_samples,
     fa.y_frames = p->max_frames;
     fa.ytile = p->ytile;
     fa.y_fmt = spectra_format(p->xmode);
+    fa.fplan = p->fplan;
     fa.y_scale = spectra_scale(p->n_freq);
     fa.err = p->d_err;
     return fengine_launch(p->n_freq, p->tw, fa, p->num_sms, static_cast<cudaStream_t>(stream));
@@ -319,7 +321,10 @@ extern "C" corr_status corrx_run_xengine(void *eng, int32_t frames, void *d_acc,
 
 namespace corrgb {
 
-corr_status fxplan_set_tiles(FxPlan *p, int ytile, int xct, int xkt) {
+corr_status fxplan_set_tiles(FxPlan *p, int ytile, int xct, int xkt, int fplan) {
+    if (fplan < 0 || fplan >= fengine_plans(p->n_freq))
+        return failf(CORR_ERR_ARG, "FFT plan %d: n_freq=%d has plans 0..%d", fplan, p->n_freq,
+                     fengine_plans(p->n_freq) - 1);
     if (ytile < 2 || ytile > p->n_freq || (ytile & (ytile - 1)) != 0)
         return failf(CORR_ERR_ARG, "ytile=%d is not a power of two in [2, n_freq=%d]", ytile,
                      p->n_freq);
@@ -340,6 +345,7 @@ corr_status fxplan_set_tiles(FxPlan *p, int ytile, int xct, int xkt) {
         p->xkt = xkt;
     }
     p->ytile = ytile;
+    p->fplan = fplan;
     return CORR_OK;
 }
 
@@ -407,38 +413,47 @@ corr_status fxplan_autotune(FxPlan *p, cudaStream_t stream, corrx_tiles *out) {
                                  stream);
     };
     auto run_x = [&] { return corrx_run_xengine(p, frames, d_acc, stream); };
-    float best_total = 1e30f, best_f = 0.f, best_x = 0.f;
+    // The F-engine's time depends on the layout and the FFT plan, the
+    // X-engine's on the layout and the tile: time each pair once.
+    const int fplan0 = p->fplan;
+    const int n_fplans = fengine_plans(p->n_freq);
+    float best_f = 1e30f, best_x = 1e30f;
+    int best_fplan = fplan0;
     Cand best{ytile0, ct0, kt0};
-    int f_ytile = -1;
-    float f_ms = 0.f;
-    for (const Cand &c : cands) {
-        if (fxplan_set_tiles(p, c.ytile, c.ct, c.kt) != CORR_OK) continue;   // not for this form
-        if (c.ytile != f_ytile) {   // the F-engine depends on the layout only
-            if ((st = timed(run_f, &f_ms)) != CORR_OK) break;
-            f_ytile = c.ytile;
-        } else if ((st = run_f()) != CORR_OK) {
-            break;
+    const int ytile = p->n_freq;   // every candidate uses contiguous rows
+    for (int fp = 0; fp < n_fplans && st == CORR_OK; ++fp) {
+        if ((st = fxplan_set_tiles(p, ytile, cands[0].ct, cands[0].kt, fp)) != CORR_OK) break;
+        float f_ms = 0.f;
+        if ((st = timed(run_f, &f_ms)) != CORR_OK) break;
+        if (f_ms < best_f) {
+            best_f = f_ms;
+            best_fplan = fp;
         }
+    }
+    for (const Cand &c : cands) {
+        if (st != CORR_OK) break;
+        if (fxplan_set_tiles(p, c.ytile, c.ct, c.kt, best_fplan) != CORR_OK)
+            continue;   // not for this form
+        if ((st = run_f()) != CORR_OK) break;   // the spectra this form reads
         float x_ms = 0.f;
         if ((st = timed(run_x, &x_ms)) != CORR_OK) break;
-        if (f_ms + x_ms < best_total) {
-            best_total = f_ms + x_ms;
-            best = c;
-            best_f = f_ms;
+        if (x_ms < best_x) {
             best_x = x_ms;
+            best = c;
         }
     }
     corr_status st_check = st == CORR_OK ? fxplan_check(p) : st;
     cleanup();
     if (st_check != CORR_OK) {
-        fxplan_set_tiles(p, ytile0, ct0, kt0);
+        fxplan_set_tiles(p, ytile0, ct0, kt0, fplan0);
         return st_check;
     }
-    if ((st = fxplan_set_tiles(p, best.ytile, best.ct, best.kt)) != CORR_OK) return st;
+    if ((st = fxplan_set_tiles(p, best.ytile, best.ct, best.kt, best_fplan)) != CORR_OK) return st;
     if (out != nullptr) {
         out->ytile = p->ytile;
         out->xct = p->xct;
         out->xkt = p->xkt;
+        out->fplan = p->fplan;
         out->ms_fengine = best_f;
         out->ms_xengine = best_x;
     }
@@ -456,6 +471,7 @@ extern "C" corr_status corrx_get_tiles(void *eng, corrx_tiles *out) {
     out->ytile = p->ytile;
     out->xct = p->xct;
     out->xkt = p->xkt;
+    out->fplan = p->fplan;
     out->ms_fengine = 0.f;
     out->ms_xengine = 0.f;
     return CORR_OK;
@@ -467,7 +483,7 @@ extern "C" corr_status corrx_set_tiles(void *eng, const corrx_tiles *t) {
     if (t->struct_size != sizeof(corrx_tiles))
         return failf(CORR_ERR_ABI, "corrx_tiles.struct_size=%u, expected %zu", t->struct_size,
                      sizeof(corrx_tiles));
-    return fxplan_set_tiles(p, t->ytile, t->xct, t->xkt);
+    return fxplan_set_tiles(p, t->ytile, t->xct, t->xkt, t->fplan);
 }
 
 extern "C" corr_status corrx_autotune(void *eng, void *stream, corrx_tiles *out) {

@@ -101,6 +101,7 @@ struct FengineArgs {
     int y_frames;               // frames the spectra buffer holds
     int ytile;                  // channels per spectra tile
     int y_fmt;                  // SpectraFormat of the stored bins (scaled by y_scale if FP16)
+    int fplan;                  // FFT radix plan (0 .. fengine_plans(n_freq) - 1)
     float y_scale;
     int *err;
 };
@@ -120,6 +121,8 @@ struct XengineArgs {
 
 // fengine.cu
 corr_status fengine_prepare(int n_freq, TwiddleTables *tw);
+/// How many FFT radix plans the F-engine has for n_freq (plan 0 always exists).
+int fengine_plans(int n_freq);
 void fengine_release(TwiddleTables *tw);
 corr_status fengine_launch(int n_freq, const TwiddleTables &tw, const FengineArgs &a,
                            int num_sms, cudaStream_t stream);
@@ -153,6 +156,7 @@ struct FxPlan {
     int ytile = 0;        // channels per spectra tile (n_freq: contiguous rows)
     int xct = 0;          // tensor X-engine: channels per tile
     int xkt = 0;          // tensor X-engine: frames per stage
+    int fplan = 0;        // F-engine FFT radix plan
     int xmode = CORR_X_PLAIN_FP32;
     int num_sms = 0;
     float2 *d_y = nullptr;
@@ -163,7 +167,7 @@ struct FxPlan {
 corr_status fxplan_create(int device, int n_station, int n_freq, int max_frames, int xmode,
                           FxPlan **out);
 void fxplan_destroy(FxPlan *p);
-corr_status fxplan_set_tiles(FxPlan *p, int ytile, int xct, int xkt);
+corr_status fxplan_set_tiles(FxPlan *p, int ytile, int xct, int xkt, int fplan);
 corr_status fxplan_autotune(FxPlan *p, cudaStream_t stream, corrx_tiles *out);
 
 /// F then X over `frames` frames, in passes of at most max_frames.

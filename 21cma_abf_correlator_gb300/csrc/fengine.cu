@@ -159,22 +159,27 @@ __device__ __forceinline__ void apply_twiddles(float2 *v, int u, const float2 *l
 // Radix plan per transform length M = 2^LOGM: three passes R0 x R1 x R2 = M,
 // P = 2*R2 points per thread, T = M/P threads. The last pass (radix R2) is
 // fused with the real-FFT split: thread t owns butterflies t and J - t
-// (J = M/R2), so Z[k] and Z[M-k] meet in its registers.
-template <int LOGM>
+// (J = M/R2), so Z[k] and Z[M-k] meet in its registers. Plan 0 has three
+// passes (R0 x R1 x R2, R1b = 1); plan 1, where a size has one, has four
+// (R0 x R1 x R1b x R2) with half the points per thread and twice the threads:
+// one more shared-memory pass against twice the warps to hide latency. The
+// autotuner times both.
+template <int LOGM, int PLAN>
 struct FePlan;
-template <> struct FePlan<14> { static constexpr int R0 = 32, R1 = 32, R2 = 16; };
-template <> struct FePlan<13> { static constexpr int R0 = 32, R1 = 16, R2 = 16; };
-template <> struct FePlan<12> { static constexpr int R0 = 16, R1 = 16, R2 = 16; };
-template <> struct FePlan<11> { static constexpr int R0 = 16, R1 = 8, R2 = 16; };
-template <> struct FePlan<10> { static constexpr int R0 = 16, R1 = 8, R2 = 8; };
-template <> struct FePlan<9> { static constexpr int R0 = 16, R1 = 4, R2 = 8; };
+template <> struct FePlan<14, 0> { static constexpr int R0 = 32, R1 = 32, R1b = 1, R2 = 16; };
+template <> struct FePlan<14, 1> { static constexpr int R0 = 16, R1 = 16, R1b = 8, R2 = 8; };
+template <> struct FePlan<13, 0> { static constexpr int R0 = 32, R1 = 16, R1b = 1, R2 = 16; };
+template <> struct FePlan<12, 0> { static constexpr int R0 = 16, R1 = 16, R1b = 1, R2 = 16; };
+template <> struct FePlan<11, 0> { static constexpr int R0 = 16, R1 = 8, R1b = 1, R2 = 16; };
+template <> struct FePlan<10, 0> { static constexpr int R0 = 16, R1 = 8, R1b = 1, R2 = 8; };
+template <> struct FePlan<9, 0> { static constexpr int R0 = 16, R1 = 4, R1b = 1, R2 = 8; };
 
-template <int LOGM>
+template <int LOGM, int PLAN>
 struct FeCfg {
-    using Plan = FePlan<LOGM>;
+    using Plan = FePlan<LOGM, PLAN>;
     static constexpr int M = 1 << LOGM;
-    static constexpr int R0 = Plan::R0, R1 = Plan::R1, R2 = Plan::R2;
-    static_assert(R0 * R1 * R2 == M, "radix plan must cover M");
+    static constexpr int R0 = Plan::R0, R1 = Plan::R1, R1b = Plan::R1b, R2 = Plan::R2;
+    static_assert(R0 * R1 * R1b * R2 == M, "radix plan must cover M");
     static constexpr int P = 2 * R2;                // points per thread
     static constexpr int T = M / P;                 // threads per CTA
     static constexpr int J = M / R2;                // butterflies of the last pass
@@ -194,9 +199,9 @@ struct FeCfg {
     static constexpr int OFF_FLAG = OFF_BAR + 16;
     static constexpr int SMEM = OFF_FLAG + 16;
     // CTAs per SM the launch bounds plan for: as many as shared memory allows,
-    // with at most 128 registers per thread.
+    // with at most 128 registers per thread (64 at 1024 threads).
     static constexpr int BY_SMEM = (220 * 1024) / SMEM;
-    static constexpr int BY_REGS = 65536 / (T * 128);
+    static constexpr int BY_REGS = T >= 1024 ? 1 : 65536 / (T * 128);
     static constexpr int MIN_BLOCKS =
         (BY_SMEM < BY_REGS ? BY_SMEM : BY_REGS) < 1 ? 1 : (BY_SMEM < BY_REGS ? BY_SMEM : BY_REGS);
 };
@@ -328,12 +333,12 @@ __device__ __forceinline__ void split_store(float2 zk, float2 zmk, float2 w, int
 // warp diverges; only X[M/2] = conj(Z[M/2]) is one extra store for thread 0.
 // Split twiddles: k = j + i*J gives w_k = w_j * exp(-pi*i*i/R2), one table
 // lookup per butterfly times compile-time constants.
-template <int LOGM, class Row>
+template <int LOGM, int PLAN, class Row>
 __device__ __forceinline__ void last_pass_store(const float2 *__restrict__ sd,
                                                 const float2 *plo, const float2 *phi,
                                                 const float2 *qlo, const float2 *qhi,
                                                 const Row &yrow, int tid) {
-    using C = FeCfg<LOGM>;
+    using C = FeCfg<LOGM, PLAN>;
     constexpr int M = C::M, J = C::J, R = C::R2, H = R / 2;
     static_assert(J % (1 << C::PADSHIFT) == 0, "last-pass stride");
     constexpr int PJ = J + (J >> C::PADSHIFT);
@@ -387,10 +392,10 @@ __device__ __forceinline__ bool frame_present(const FengineArgs &a, int f, int s
     return (byte >> (bit & 7)) & 1u;
 }
 
-template <int LOGM, int FMT, bool CONTIG>
-__global__ void __launch_bounds__(FeCfg<LOGM>::T, FeCfg<LOGM>::MIN_BLOCKS)
+template <int LOGM, int PLAN, int FMT, bool CONTIG>
+__global__ void __launch_bounds__(FeCfg<LOGM, PLAN>::T, FeCfg<LOGM, PLAN>::MIN_BLOCKS)
     fengine_kernel(FengineArgs a, TwPtrs tw) {
-    using C = FeCfg<LOGM>;
+    using C = FeCfg<LOGM, PLAN>;
     constexpr int M = C::M;
     constexpr int T = C::T;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -489,26 +494,29 @@ __global__ void __launch_bounds__(FeCfg<LOGM>::T, FeCfg<LOGM>::MIN_BLOCKS)
         }
         fft_pass<M, T, C::P, C::R1, C::R0, C::PADSHIFT, false, true>(sd, nullptr, plo, phi, tid,
                                                                     t2);
-        last_pass_store<LOGM>(sd, plo, phi, qlo, qhi, yrow, tid);
+        if constexpr (C::R1b > 1)
+            fft_pass<M, T, C::P, C::R1b, C::R0 * C::R1, C::PADSHIFT, false>(sd, nullptr, plo, phi,
+                                                                          tid);
+        last_pass_store<LOGM, PLAN>(sd, plo, phi, qlo, qhi, yrow, tid);
         // The next item's first pass synchronises before it overwrites sd.
     }
 }
 
-template <int LOGM, int FMT, bool CONTIG>
+template <int LOGM, int PLAN, int FMT, bool CONTIG>
 corr_status launch_one(const FengineArgs &a, const TwiddleTables &tw, int num_sms,
                        cudaStream_t stream) {
-    using C = FeCfg<LOGM>;
+    using C = FeCfg<LOGM, PLAN>;
     static bool configured = false;
     static int per_sm = 1;
     if (!configured) {
         corr_status st = cuda_check(
-            cudaFuncSetAttribute(fengine_kernel<LOGM, FMT, CONTIG>,
+            cudaFuncSetAttribute(fengine_kernel<LOGM, PLAN, FMT, CONTIG>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM),
             "cudaFuncSetAttribute(fengine)");
         if (st != CORR_OK) return st;
         int blocks = 0;
         st = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                            &blocks, fengine_kernel<LOGM, FMT, CONTIG>, C::T, C::SMEM),
+                            &blocks, fengine_kernel<LOGM, PLAN, FMT, CONTIG>, C::T, C::SMEM),
                         "cudaOccupancyMaxActiveBlocksPerMultiprocessor(fengine)");
         if (st != CORR_OK) return st;
         if (blocks < 1)
@@ -521,22 +529,33 @@ corr_status launch_one(const FengineArgs &a, const TwiddleTables &tw, int num_sm
     int grid = num_sms * per_sm;
     if (grid > items) grid = items;
     TwPtrs p{tw.pass_lo, tw.pass_hi, tw.post_lo, tw.post_hi};
-    fengine_kernel<LOGM, FMT, CONTIG><<<grid, C::T, C::SMEM, stream>>>(a, p);
+    fengine_kernel<LOGM, PLAN, FMT, CONTIG><<<grid, C::T, C::SMEM, stream>>>(a, p);
     return cuda_check(cudaGetLastError(), "fengine_kernel launch");
 }
 
-template <int LOGM>
-corr_status launch_size(const FengineArgs &a, const TwiddleTables &tw, int num_sms,
+template <int LOGM, int PLAN>
+corr_status launch_plan(const FengineArgs &a, const TwiddleTables &tw, int num_sms,
                         cudaStream_t stream) {
     const bool contig = a.ytile == (1 << LOGM);
     if (a.y_fmt != kSpectraF32) {
         if (!contig)
             return fail(CORR_ERR_ARG, "FP16 spectra are written as contiguous rows (ytile = n_freq)");
-        if (a.y_fmt == kSpectraF16) return launch_one<LOGM, kSpectraF16, true>(a, tw, num_sms, stream);
-        return launch_one<LOGM, kSpectraF16Split, true>(a, tw, num_sms, stream);
+        if (a.y_fmt == kSpectraF16) return launch_one<LOGM, PLAN, kSpectraF16, true>(a, tw, num_sms, stream);
+        return launch_one<LOGM, PLAN, kSpectraF16Split, true>(a, tw, num_sms, stream);
     }
-    if (contig) return launch_one<LOGM, kSpectraF32, true>(a, tw, num_sms, stream);
-    return launch_one<LOGM, kSpectraF32, false>(a, tw, num_sms, stream);
+    if (contig) return launch_one<LOGM, PLAN, kSpectraF32, true>(a, tw, num_sms, stream);
+    return launch_one<LOGM, PLAN, kSpectraF32, false>(a, tw, num_sms, stream);
+}
+
+template <int LOGM>
+corr_status launch_size(const FengineArgs &a, const TwiddleTables &tw, int num_sms,
+                        cudaStream_t stream) {
+    if constexpr (LOGM == 14) {
+        if (a.fplan == 1) return launch_plan<LOGM, 1>(a, tw, num_sms, stream);
+    }
+    if (a.fplan != 0)
+        return failf(CORR_ERR_ARG, "FFT plan %d is not available at n_freq=%d", a.fplan, 1 << LOGM);
+    return launch_plan<LOGM, 0>(a, tw, num_sms, stream);
 }
 
 int ilog2(int v) {
@@ -546,6 +565,8 @@ int ilog2(int v) {
 }
 
 } // namespace
+
+int fengine_plans(int n_freq) { return n_freq == 16384 ? 2 : 1; }
 
 corr_status fengine_prepare(int n_freq, TwiddleTables *tw) {
     const int M = n_freq;

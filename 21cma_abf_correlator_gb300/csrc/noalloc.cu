@@ -153,6 +153,7 @@ extern "C" corr_status corrx_accumulate_noalloc(int32_t n_station, int32_t n_fre
     fa.y_frames = frames;
     fa.ytile = n_freq;
     fa.y_fmt = spectra_format(xmode);
+    fa.fplan = 0;
     fa.y_scale = spectra_scale(n_freq);
     fa.err = nullptr;
     if ((st = fengine_launch(n_freq, tw, fa, d.num_sms, s)) != CORR_OK) return st;

@@ -86,10 +86,11 @@ class FxEngine:
         """Current (ytile, xct, xkt): spectra tile width and tensor X tile shape."""
         t = abi.corrx_tiles(struct_size=C.sizeof(abi.corrx_tiles))
         abi.check(self.lib.corrx_get_tiles(self.h, C.byref(t)), "corrx_get_tiles")
-        return {"ytile": t.ytile, "xct": t.xct, "xkt": t.xkt}
+        return {"ytile": t.ytile, "xct": t.xct, "xkt": t.xkt, "fplan": t.fplan}
 
-    def set_tiles(self, ytile: int, xct: int = 0, xkt: int = 0) -> None:
-        t = abi.corrx_tiles(struct_size=C.sizeof(abi.corrx_tiles), ytile=ytile, xct=xct, xkt=xkt)
+    def set_tiles(self, ytile: int, xct: int = 0, xkt: int = 0, fplan: int = 0) -> None:
+        t = abi.corrx_tiles(struct_size=C.sizeof(abi.corrx_tiles), ytile=ytile, xct=xct, xkt=xkt,
+                            fplan=fplan)
         abi.check(self.lib.corrx_set_tiles(self.h, C.byref(t)), "corrx_set_tiles")
 
     def autotune(self, stream=None) -> dict:
@@ -97,5 +98,5 @@ class FxEngine:
         t = abi.corrx_tiles(struct_size=C.sizeof(abi.corrx_tiles))
         abi.check(self.lib.corrx_autotune(self.h, C.c_void_p(_stream_handle(stream)), C.byref(t)),
                   "corrx_autotune")
-        return {"ytile": t.ytile, "xct": t.xct, "xkt": t.xkt,
+        return {"ytile": t.ytile, "xct": t.xct, "xkt": t.xkt, "fplan": t.fplan,
                 "ms_fengine": t.ms_fengine, "ms_xengine": t.ms_xengine}

@@ -87,6 +87,8 @@ typedef struct corrx_tiles {
     int32_t  ytile;
     int32_t  xct;
     int32_t  xkt;
+    int32_t  fplan;       /* F-engine FFT radix plan: 0 (three passes), or 1 at
+                             n_freq 16384 (four passes, twice the threads)        */
     float    ms_fengine;  /* corrx_autotune: F-engine ms per max_frames pass       */
     float    ms_xengine;  /* corrx_autotune: X-engine ms per max_frames pass       */
 } corrx_tiles;
@@ -95,10 +97,11 @@ corr_status corrx_get_tiles(void *eng, corrx_tiles *out);
 /* CORR_ERR_ARG for an infeasible shape; the spectra buffer's previous contents
    become meaningless (run the F-engine again). */
 corr_status corrx_set_tiles(void *eng, const corrx_tiles *t);
-/* Time every feasible (ytile, xct, xkt) on this device -- one F-engine and one
-   X-engine pass of max_frames synthetic frames each (temporary device buffers of
-   n_station*max_frames*2*n_freq bytes plus one row) -- keep the fastest F+X
-   pair and report it in *out (may be NULL). Synchronises `stream`. */
+/* Time every FFT plan and every feasible (ytile, xct, xkt) on this device -- F-
+   and X-engine passes of min(max_frames, 1024) synthetic frames (temporary
+   device buffers of that many frames plus one row) -- keep the fastest F-engine
+   plan and X-engine tile and report them in *out (may be NULL). Synchronises
+   `stream`. */
 corr_status corrx_autotune(void *eng, void *stream, corrx_tiles *out);
 
 /* corrx_autotune for the engine inside an ABI context; allowed only while no

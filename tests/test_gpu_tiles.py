@@ -105,11 +105,12 @@ def test_autotune_picks_a_feasible_shape_with_same_results(pkg, cuda, oracle, xm
         t = eng.autotune()
         assert t["ms_fengine"] > 0 and t["ms_xengine"] > 0
         eng.check()
-        tiles = (t["ytile"], t["xct"], t["xkt"])
-        assert eng.tiles() == {"ytile": t["ytile"], "xct": t["xct"], "xkt": t["xkt"]}
+        tiles = (t["ytile"], t["xct"], t["xkt"], t["fplan"])
+        assert eng.tiles() == {k: t[k] for k in ("ytile", "xct", "xkt", "fplan")}
     finally:
         eng.close()
     got = _run(pkg, cuda, x, mask, xmode, tiles)
+    # n_freq 2048 has one FFT plan: the same plan, only the tile may differ
     assert np.array_equal(got, base)
     print(f"xmode={xmode}: autotune chose {t}")
 
@@ -120,3 +121,33 @@ def test_autotune_through_abi_golden(pkg, cuda, oracle):
     got = drive_rows(pkg, x, int(fx["n_cum"]), int(fx["frames_per_slot"]), xmode=2, autotune=True)
     rms = oracle.rel_rms(got[:, :, fx["channels"]], fx["expect_subset"])
     assert rms <= tol(2, int(fx["n_cum"]))["rms"]
+
+
+@pytest.mark.parametrize("xmode", [0, 2])
+def test_both_fft_plans_match_the_oracle(pkg, cuda, oracle, xmode):
+    """n_freq 16384 has a three-pass and a four-pass FFT plan; both are exact to FP32."""
+    n, nf, frames = 6, 16384, 24
+    x, present, mask = _case(n, nf, frames, 21)
+    ref = oracle.correlate(x, present)
+    outs = []
+    for fplan in (0, 1):
+        eng = pkg.FxEngine(n, nf, max_frames=32, xmode=xmode)
+        t = eng.tiles()
+        eng.close()
+        got = _run(pkg, cuda, x, mask, xmode, (t["ytile"], t["xct"], t["xkt"], fplan))
+        assert oracle.rel_rms(got, ref) < 1e-5, f"plan {fplan}"
+        assert oracle.normalized_max_err(got, ref, n) < 2e-5, f"plan {fplan}"
+        outs.append(got)
+    assert oracle.rel_rms(outs[0], outs[1]) < 1e-5
+
+
+def test_unknown_fft_plan_is_refused(pkg, cuda):
+    eng = pkg.FxEngine(4, 1024, max_frames=8, xmode=0)
+    try:
+        t = eng.tiles()
+        with pytest.raises(pkg.abi.CorrError):
+            eng.set_tiles(t["ytile"], t["xct"], t["xkt"], 1)   # n_freq 1024 has one plan
+        with pytest.raises(pkg.abi.CorrError):
+            eng.set_tiles(t["ytile"], t["xct"], t["xkt"], -1)
+    finally:
+        eng.close()
