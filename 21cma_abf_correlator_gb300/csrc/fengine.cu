@@ -133,22 +133,25 @@ __device__ __forceinline__ void apply_twiddles(float2 *v, int u, const float2 *l
                                                const float2 *hi) {
     float2 w[R];
     w[1] = tw_pass(lo, hi, u);
+    // w^4, w^8, w^16: lo[(k*u) & 63] = lo[k*(u & (64/k - 1))], read from the
+    // compact copies lo[64 + ...] (k = 4), lo[80 + ...] (8), lo[88 + ...] (16)
+    // so that a warp's lanes hit distinct banks
     if constexpr (R >= 4) {
         w[2] = cmul(w[1], w[1]);
         w[3] = cmul(w[2], w[1]);
     }
     if constexpr (R >= 8) {
-        w[4] = tw_pass(lo, hi, 4 * u);
+        w[4] = cmul(lo[64 + (u & 15)], hi[(4 * u) >> 6]);
 #pragma unroll
         for (int r = 5; r < 8; ++r) w[r] = cmul(w[4], w[r - 4]);
     }
     if constexpr (R >= 16) {
-        w[8] = tw_pass(lo, hi, 8 * u);
+        w[8] = cmul(lo[80 + (u & 7)], hi[(8 * u) >> 6]);
 #pragma unroll
         for (int r = 9; r < 16; ++r) w[r] = cmul(w[8], w[r - 8]);
     }
     if constexpr (R >= 32) {
-        w[16] = tw_pass(lo, hi, 16 * u);
+        w[16] = cmul(lo[88 + (u & 3)], hi[(16 * u) >> 6]);
 #pragma unroll
         for (int r = 17; r < 32; ++r) w[r] = cmul(w[16], w[r - 16]);
     }
@@ -191,7 +194,7 @@ struct FeCfg {
     static constexpr int OFF_X1 = 2 * M;               // int8 frame, buffer 1
     static constexpr int OFF_D = 4 * M;                // padded complex data
     static constexpr int OFF_PLO = OFF_D + (M + (M >> PADSHIFT)) * 8;
-    static constexpr int OFF_PHI = OFF_PLO + 64 * 8;
+    static constexpr int OFF_PHI = OFF_PLO + 92 * 8;   // lo[64] + lo4[16] + lo8[8] + lo16[4]
     static constexpr int OFF_QLO = OFF_PHI + N_PASS_HI * 8;
     static constexpr int OFF_QHI = OFF_QLO + 64 * 8;
     static constexpr int OFF_T2 = OFF_QHI + N_POST_HI * 8;   // second-pass twiddles
@@ -415,6 +418,9 @@ __global__ void __launch_bounds__(FeCfg<LOGM, PLAN>::T, FeCfg<LOGM, PLAN>::MIN_B
         plo[i] = tw.pass_lo[i];
         qlo[i] = tw.post_lo[i];
     }
+    for (int i = tid; i < 28; i += T)   // compact copies for w^4, w^8, w^16
+        plo[64 + i] = i < 16 ? tw.pass_lo[4 * i] : i < 24 ? tw.pass_lo[8 * (i - 16)]
+                                                           : tw.pass_lo[16 * (i - 24)];
     for (int i = tid; i < C::N_PASS_HI; i += T) phi[i] = tw.pass_hi[i];
     for (int i = tid; i < C::N_POST_HI; i += T) qhi[i] = tw.post_hi[i];
     // second pass: t2[r][jj] = exp(-2*pi*i*r*jj/(R0*R1)) = w^u, u = r*jj*M/(R0*R1)
