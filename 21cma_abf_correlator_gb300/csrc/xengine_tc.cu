@@ -94,7 +94,7 @@ struct TcGeom {
     bool split;
     int ct;            // channels per tile
     int kt;            // frames per stage (16 or 32)
-    int R;             // rows of one channel's D (2N rounded up to 8)
+    int R;             // first row of a region's second block (>= 2N, a multiple of 8)
     int nb;            // MMA N
     int regions;       // operand regions per stage
     int sbo;           // bytes between 8-row groups = (kt/8) * 128
@@ -139,15 +139,20 @@ TcGeom make_geom(int n_station, bool split, int ct, int kt) {
     g.elem = split ? 8 : 4;
     if (ct * g.elem < 16) return g;
     g.R = round_up(2 * N, 8);
+    // A region's second block (Dl, or the second channel) starts at row 64
+    // when it fits: its accumulator rows then fall in TMEM lane quarters 2-3,
+    // so the four epilogue warps share the read-out evenly.
+    const bool stacks = g.R + 2 * N <= 128;
+    if (stacks) g.R = std::max(g.R, 64);
     int rows_valid;
     if (split) {
-        g.form = (g.R + 2 * N <= 128) ? kSplitStacked : kSplitWide;
+        g.form = stacks ? kSplitStacked : kSplitWide;
         g.nb = g.form == kSplitStacked ? std::max(16, round_up(2 * N, 16))
                                        : round_up(g.R + 2 * N, 16);
         g.regions = ct;
         rows_valid = g.R + 2 * N;
     } else {
-        g.form = (g.R + 2 * N <= 128) ? kFp16Paired : kFp16Wide;
+        g.form = stacks ? kFp16Paired : kFp16Wide;
         g.nb = g.form == kFp16Paired ? round_up(g.R + 2 * N, 16)
                                      : std::max(16, round_up(2 * N, 16));
         g.regions = g.form == kFp16Paired ? ct / 2 : ct;
