@@ -3,7 +3,7 @@
 Workload (default): 24 inputs, n_freq 16384 (32768-sample frames), 4096 frames
 per integration -- the precision workload the throughput target is quoted on.
 A step is one integration: zero the accumulator, F-engine + X-engine over all
-4096 frames (passes of 256 frames), scale by 1/4096. Inputs (3.2 GB of int8)
+4096 frames (passes of 1024 frames), scale by 1/4096. Inputs (3.2 GB of int8)
 are generated in HBM before timing and are larger than L2, so no flush is needed.
 
   value      : device-resident throughput, int8 samples in per second (GS/s)
@@ -136,10 +136,13 @@ def _oracle_worker(args):
 def time_cpu_oracle(w, target_s: float, processes: int) -> dict:
     """Time the float64 oracle on frames of this workload, spread over `processes`."""
     L = w.fft_len
-    # calibrate on one frame in this process
-    probe = _oracle_worker((w.name, 1, 0))
-    per_frame = max(probe, 1e-4)
-    frames_per_proc = max(1, int(target_s / per_frame / 1.2))
+    # calibrate in this process: one warm call (first-call costs), then the
+    # marginal cost per frame between 4 and 16 frames
+    _oracle_worker((w.name, 1, 0))
+    t4 = _oracle_worker((w.name, 4, 0))
+    t16 = _oracle_worker((w.name, 16, 0))
+    per_frame = max((t16 - t4) / 12, t16 / 32, 1e-4)
+    frames_per_proc = max(1, int(target_s / per_frame))
     frames_per_proc = min(frames_per_proc, 512)
     if processes <= 1:
         wall = _oracle_worker((w.name, frames_per_proc, 1))
@@ -207,6 +210,9 @@ def main() -> None:
                     help="frames per F/X pass (spectra buffer depth)")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the default tile shapes instead of autotuning them")
+    ap.add_argument("--tiles", default="",
+                    help="XCT,XKT,FPLAN: fixed tensor tile and FFT plan instead of the "
+                         "autotuner's (profiling a chosen configuration)")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the batching and stream workloads")
     args = ap.parse_args()
@@ -268,7 +274,14 @@ def main() -> None:
     for name in candidates:
         try:
             eng = pkg.FxEngine(N, nf, PASS_FRAMES, xmode=modes[name])
-            tiles[name] = eng.autotune(stream) if not args.no_tune else eng.tiles()
+            if args.tiles:
+                xct, xkt, fplan = (int(v) for v in args.tiles.split(","))
+                eng.set_tiles(nf, xct, xkt, fplan)
+                tiles[name] = eng.tiles()
+            elif args.no_tune:
+                tiles[name] = eng.tiles()
+            else:
+                tiles[name] = eng.autotune(stream)
             acc = eng.new_acc()
             step = make_step(eng, acc)
             step()
@@ -323,7 +336,7 @@ def main() -> None:
     for name, (e_, a_, s_) in engines.items():
         m = ms if name == best else time_steps(s_, max(2, args.steps // 2), 1)
         paths[name] = {"value": samples_step / (m * 1e-3) / 1e9, "ms_per_step": m,
-                       "tiles": {k: tiles[name][k] for k in ("ytile", "xct", "xkt")},
+                       "tiles": {k: tiles[name][k] for k in ("ytile", "xct", "xkt", "fplan")},
                        "per_vis_err_bound": err_bound[name]}
 
     # per-kernel times: one pass of PASS_FRAMES frames through each kernel alone
@@ -430,10 +443,10 @@ def main() -> None:
 # traffic is all per frame (int8 read, spectra write); the X-engines' is the
 # spectra read (per frame) plus the row's read and write (per launch).
 _NCU_256 = {
-    "fengine": {"tc": (543.655168e6, 0.0), "tc_split": (944.579584e6, 0.0),
-                "plain": (945.517056e6, 0.0)},
-    "xengine": {"tc": (402.653184e6, 69.501e6), "tc_split": (805.306368e6, 75.578e6),
-                "plain": (805.306368e6, 73.406e6)},
+    "fengine": {"tc": (543.183616e6, 0.0), "tc_split": (944.986112e6, 0.0),
+                "plain": (945.010432e6, 0.0)},
+    "xengine": {"tc": (402.653184e6, 69.404160e6), "tc_split": (805.306368e6, 74.243584e6),
+                "plain": (805.306368e6, 73.059328e6)},
 }
 
 
@@ -519,7 +532,7 @@ def run_stream(pkg, synth, torch, stream) -> dict:
     gs = w.n_station * w.frames * w.fft_len / (ms * 1e-3) / 1e9
     need = w.n_station * 0.25
     return {"workload": w.name, "xengine": "tc_split", "value": gs, "unit": "GSample/s",
-            "tiles": {k: tiles[k] for k in ("ytile", "xct", "xkt")},
+            "tiles": {k: tiles[k] for k in ("ytile", "xct", "xkt", "fplan")},
             "ms_per_integration": ms, "real_time_factor": gs / need,
             "real_time_need_gsps": need,
             "integrations_per_60s": 60.0 * 250e6 / (w.frames * w.fft_len)}
