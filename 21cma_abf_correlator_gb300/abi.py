@@ -113,6 +113,90 @@ class corrx_tiles(C.Structure):
     ]
 
 
+CORRX_PATTERN_ZERO, CORRX_PATTERN_COUNTER, CORRX_PATTERN_PRNG, CORRX_PATTERN_SINE = 0, 1, 2, 3
+CORRX_FRONTEND_MAX_STATIONS = 64
+
+
+class corrx_frontend(C.Structure):
+    """The synthetic front end's settings (corr_gb300.h), one field per option of
+    the reference's transmitter (corr-rs/src/bin/replay.rs:41-165)."""
+    _fields_ = [
+        ("struct_size", C.c_uint32),
+        ("pattern", C.c_int32),
+        ("seed", C.c_uint64),
+        ("tone", C.c_double),
+        ("start_counter", C.c_uint64),
+        ("n_packets", C.c_uint64),
+        ("drop_rate", C.c_double),
+        ("gap_at", C.c_uint64),
+        ("gap_len", C.c_uint64),
+        ("ladder_frames", C.c_uint64),
+        ("ladder_steps", C.c_uint64),
+        ("sample_delay", C.c_int64 * CORRX_FRONTEND_MAX_STATIONS),
+        ("counter_offset", C.c_uint64 * CORRX_FRONTEND_MAX_STATIONS),
+    ]
+
+
+CORRW_SET_AUTO, CORRW_SET_NEW, CORRW_SET_EXPLICIT = 0, 1, 2
+CORRW_QUEUE_DROP, CORRW_QUEUE_BLOCK = 0, 1
+
+
+class corrw_station(C.Structure):
+    _fields_ = [
+        ("name", C.c_char_p),
+        ("group_ip", C.c_char_p),
+        ("dest_port", C.c_int32),
+        ("board", C.c_char_p),
+    ]
+
+
+class corrw_params(C.Structure):
+    """Output file-set writer settings (corr_writer.h; reference corr-rs/src/writer.rs)."""
+    _fields_ = [
+        ("struct_size", C.c_uint32),
+        ("n_station", C.c_int32),
+        ("n_freq", C.c_int32),
+        ("n_cum", C.c_uint32),
+        ("frames_per_slot", C.c_uint32),
+        ("rows_per_fetch", C.c_uint32),
+        ("sample_rate_hz", C.c_uint64),
+        ("data_shift_count", C.c_int32),
+        ("daily_files", C.c_int32),
+        ("set_policy", C.c_int32),
+        ("queue_full", C.c_int32),
+        ("queue_rows", C.c_uint32),
+        ("fsync_every_rows", C.c_uint32),
+        ("dir", C.c_char_p),
+        ("file_prefix", C.c_char_p),
+        ("file_prefix_format", C.c_char_p),
+        ("config_version", C.c_char_p),
+        ("config_hash", C.c_char_p),
+        ("set_tag", C.c_char_p),
+        ("stations", C.POINTER(corrw_station)),
+    ]
+
+
+class corrw_resume(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_uint32),
+        ("has_next_frame_id", C.c_uint32),
+        ("rows_written", C.c_uint64),
+        ("truncated_rows", C.c_uint64),
+        ("next_frame_id", C.c_uint64),
+    ]
+
+
+class corrw_stats(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_uint32),
+        ("sets_opened", C.c_uint32),
+        ("rows_written", C.c_uint64),
+        ("rows_dropped", C.c_uint64),
+        ("max_queued", C.c_uint64),
+        ("set_tag", C.c_char * 256),
+    ]
+
+
 # Layouts pinned by the reference's Rust mirror (ffi.rs compile-time asserts).
 assert C.sizeof(corr_config) == 76
 assert C.sizeof(corr_device_plan) == 20
@@ -175,6 +259,16 @@ SIGNATURES = {
     "corrx_accumulate_noalloc": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
                                            C.c_size_t, C.c_size_t, C.c_void_p, C.c_size_t,
                                            C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "corrx_frontend_fill": (C.c_int, [C.POINTER(corrx_frontend), C.c_int32, C.c_int32,
+                                      C.c_int32, C.c_int64, C.c_int32, C.c_void_p, C.c_size_t, C.c_size_t,
+                                      C.c_void_p, C.c_size_t, C.c_void_p]),
+    "corrw_open": (C.c_int, [C.POINTER(corrw_params), C.POINTER(C.c_void_p),
+                             C.POINTER(corrw_resume)]),
+    "corrw_write_row": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int64, C.c_uint64,
+                                  C.c_uint64, C.POINTER(C.c_uint64)]),
+    "corrw_sync": (C.c_int, [C.c_void_p]),
+    "corrw_stats_get": (C.c_int, [C.c_void_p, C.POINTER(corrw_stats)]),
+    "corrw_close": (C.c_int, [C.c_void_p]),
 }
 
 _lib: C.CDLL | None = None

@@ -407,6 +407,8 @@ def main() -> None:
         torch.cuda.empty_cache()
         extra["stream"] = run_stream(pkg, synth, torch, stream)
         torch.cuda.empty_cache()
+        extra["frontend"] = run_frontend(pkg, w, torch, stream)
+        torch.cuda.empty_cache()
 
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
@@ -536,6 +538,39 @@ def run_stream(pkg, synth, torch, stream) -> dict:
             "ms_per_integration": ms, "real_time_factor": gs / need,
             "real_time_need_gsps": need,
             "integrations_per_60s": 60.0 * 250e6 / (w.frames * w.fft_len)}
+
+
+def run_frontend(pkg, w, torch, stream) -> dict:
+    """The on-device synthetic front end (corrx_frontend_fill) writing one whole
+    integration of this workload (frames + validity mask) into HBM, per pattern:
+    samples generated per second and the write bandwidth against the measured peak."""
+    fe = importlib.import_module(PKG_NAME + ".frontend")
+    N, nf, F, L = w.n_station, w.n_freq, w.frames, w.fft_len
+    x = torch.empty((N, F, L), dtype=torch.int8, device="cuda")
+    m = torch.empty((N, (F + 7) // 8), dtype=torch.uint8, device="cuda")
+    hbm, _, kind = peaks()
+    out = {"workload": w.name, "frames": F, "unit": "GSample/s", "patterns": {}}
+    for pattern in ("prng", "counter"):
+        spec = fe.ReplaySpec(pattern=pattern, drop_rate=0.001, delay_stride=1)
+        frame0 = spec.first_full_frame(nf)
+        for _ in range(2):
+            fe.fill(spec, nf, frame0, x, m, stream=stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            fe.fill(spec, nf, frame0, x, m, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 3
+        nbytes = x.numel() + m.numel()
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        out["patterns"][pattern] = {"ms": ms, "value": N * F * L / (ms * 1e-3) / 1e9,
+                                    "write_gbs": gbs, "frac_of_hbm": gbs / hbm,
+                                    "peak_kind": kind}
+    out["value"] = out["patterns"]["prng"]["value"]
+    del x, m
+    return out
 
 
 def run_e2e(pkg, w, x, mask, xmode, args, torch) -> dict:

@@ -173,6 +173,73 @@ corr_status corrx_accumulate_noalloc(int32_t n_station, int32_t n_freq, int32_t 
                                      size_t mask_station_stride, int32_t mask_bit0,
                                      int32_t frames, void *d_acc, void *stream);
 
+/*
+ * On-device synthetic front end: the traffic of the reference's test transmitter
+ * (corr-rs/src/bin/replay.rs), assembled into frames and a validity mask the way
+ * the receive side does it (corr-rs/src/assemble.rs), written straight into
+ * device memory or into the pinned staging ring.
+ *
+ * Packets: an 8-byte counter c and SAMPLES_PER_PACKET = 4096 int8 samples
+ * (corr-rs/src/config.rs:26). Frame id = c / P, P = 2*n_freq/4096 packets per
+ * frame, the packet's samples at byte (c % P)*4096 of the frame. Patterns
+ * (replay.rs:212-265), station s, sample k of the packet:
+ *   ZERO    0
+ *   COUNTER x = c*0x9E3779B97F4A7C15 + s*0x12345678; per sample x ^= x<<13,
+ *           x ^= x>>7, x ^= x<<17, sample = (x>>3) % 9 - 4
+ *   PRNG    splitmix64-style hash of the absolute sample index c*4096 + k - d_s
+ *           plus seed, sample = (h>>8) % 9 - 4 (replay.rs:212-226); d_s is the
+ *           station's sample delay (times the ladder step, below)
+ *   SINE    round(4*sin(phase + k*tone*2pi/4096)), phase = (c + seed*s)*tone*2pi,
+ *           evaluated in IEEE double without contraction
+ * Station s sends counters start_counter + counter_offset[s] + n for
+ * n < n_packets (0 = no end). Packet n is missing if gap_at <= n < gap_at +
+ * gap_len, or if the loss hash of (c, s) falls below drop_rate (replay.rs:
+ * 414-424). Ladder (ladder_frames > 0): the delay of station s in frame F is
+ * sample_delay[s]*k, k = 1 + (F - origin)/ladder_frames for F >= origin else 1,
+ * capped at ladder_steps when that is > 0, origin = the first multiple of
+ * ladder_frames at or after frame (start_counter*4096)/(2*n_freq). The time-based
+ * stall of replay.rs (a station silent for some seconds) is not modelled.
+ *
+ * corrx_frontend_fill writes frames [frame0, frame0 + frames) of stations
+ * station0 .. station0 + n_station - 1 (station indices as the transmitter numbers
+ * them, which select sample_delay[], counter_offset[] and enter the patterns and
+ * the loss hash): station station0 + s, frame f at samples + s*station_stride +
+ * f*frame_stride (any alignment; 16-byte aligned frames are written fastest;
+ * bytes of frames whose bit is clear hold the pattern, which the engines never
+ * read), and validity bit f (LSB first) of the
+ * bit string at mask + s*mask_station_stride: set iff all P packets of the frame
+ * were sent and not lost, as the receive side sets it; the bits after `frames`
+ * in the last byte are cleared. Either pointer may be NULL to skip that output;
+ * both may be device memory or pinned host memory (the staging ring, one call
+ * per station as corr_staging_info describes it). n_freq must be a multiple of
+ * 2048 (whole packets per frame), station0 + n_station <= 64.
+ */
+enum { CORRX_PATTERN_ZERO = 0, CORRX_PATTERN_COUNTER = 1, CORRX_PATTERN_PRNG = 2,
+       CORRX_PATTERN_SINE = 3 };
+#define CORRX_FRONTEND_MAX_STATIONS 64
+
+typedef struct corrx_frontend {
+    uint32_t struct_size;     /* sizeof(corrx_frontend)                            */
+    int32_t  pattern;         /* CORRX_PATTERN_*             (replay --pattern)     */
+    uint64_t seed;            /*                             (replay --seed)        */
+    double   tone;            /* SINE: cycles per sample     (replay --tone)        */
+    uint64_t start_counter;   /* first counter               (replay --start-counter) */
+    uint64_t n_packets;       /* packets per station, 0 = unbounded (duration*rate) */
+    double   drop_rate;       /* in [0, 1)                   (replay --drop-rate)   */
+    uint64_t gap_at;          /*                             (replay --gap-at)      */
+    uint64_t gap_len;         /*                             (replay --gap-len)     */
+    uint64_t ladder_frames;   /* 0 = no ladder               (replay --ladder-frames) */
+    uint64_t ladder_steps;    /* 0 = no cap                  (replay --ladder-steps) */
+    int64_t  sample_delay[CORRX_FRONTEND_MAX_STATIONS];   /* --sample-delay, or
+                                 --delay-stride * s, resolved per station          */
+    uint64_t counter_offset[CORRX_FRONTEND_MAX_STATIONS]; /* replay --offset        */
+} corrx_frontend;
+
+corr_status corrx_frontend_fill(const corrx_frontend *fe, int32_t station0, int32_t n_station,
+                                int32_t n_freq, int64_t frame0, int32_t frames, int8_t *samples,
+                                size_t station_stride, size_t frame_stride, uint8_t *mask,
+                                size_t mask_station_stride, void *stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

@@ -53,8 +53,15 @@ def test_struct_layouts_match_header(pkg, tmp_path):
         "corr_device_stats": [f for f, _ in pkg.abi.corr_device_stats._fields_],
         "corr_staging": [f for f, _ in pkg.abi.corr_staging._fields_],
         "corrx_params": [f for f, _ in pkg.abi.corrx_params._fields_],
+        "corrx_tiles": [f for f, _ in pkg.abi.corrx_tiles._fields_],
+        "corrx_frontend": [f for f, _ in pkg.abi.corrx_frontend._fields_],
+        "corrw_station": [f for f, _ in pkg.abi.corrw_station._fields_],
+        "corrw_params": [f for f, _ in pkg.abi.corrw_params._fields_],
+        "corrw_resume": [f for f, _ in pkg.abi.corrw_resume._fields_],
+        "corrw_stats": [f for f, _ in pkg.abi.corrw_stats._fields_],
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "corr_gb300.h"',
+             '#include "corr_writer.h"',
              "int main(void) {"]
     for s, fl in fields.items():
         lines.append(f'printf("{s} size %zu\\n", sizeof({s}));')
