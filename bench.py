@@ -409,6 +409,7 @@ def main() -> None:
         torch.cuda.empty_cache()
         extra["frontend"] = run_frontend(pkg, w, torch, stream)
         torch.cuda.empty_cache()
+        extra["writer"] = run_writer(pkg, w)
 
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
@@ -571,6 +572,39 @@ def run_frontend(pkg, w, torch, stream) -> dict:
     out["value"] = out["patterns"]["prng"]["value"]
     del x, m
     return out
+
+
+def run_writer(pkg, w, n_rows: int = 8) -> dict:
+    """The native file-set writer on rows of this workload (n_baseline x n_freq
+    complex64 each), into a RAM-backed directory when the host has one, with an
+    fsync per row: rows per second against the row period of the real-time
+    stream (frames x 2 n_freq samples at 250 MS/s)."""
+    import shutil
+    import tempfile
+    wr = importlib.import_module(PKG_NAME + ".writer")
+    base = "/dev/shm" if os.path.isdir("/dev/shm") else None
+    d = tempfile.mkdtemp(prefix="corr-writer-", dir=base)
+    try:
+        rng = np.random.default_rng(0)
+        rows = [rng.standard_normal((w.n_baseline, w.n_freq * 2)).astype(np.float32)
+                .view(np.complex64) for _ in range(2)]
+        names = [f"S{i:02d}" for i in range(w.n_station)]
+        t0 = time.perf_counter()
+        with wr.RowWriter(d, names, w.n_freq, w.frames, "bench", queue_rows=4,
+                          queue_full="block", fsync_every_rows=1) as wt:
+            for i in range(n_rows):
+                wt.write_row(rows[i % 2], 1_790_000_000_000 + i, i, i * w.frames,
+                             [w.frames] * w.n_station)
+            wt.sync()
+        dt = time.perf_counter() - t0
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    row_bytes = w.n_baseline * w.n_freq * 8
+    period_ms = w.frames * w.fft_len / 250e6 * 1e3
+    return {"rows": n_rows, "row_bytes": row_bytes, "ms_per_row": dt * 1e3 / n_rows,
+            "write_mbs": row_bytes * n_rows / dt / 1e6, "dir": base or "tmp",
+            "fsync_every_rows": 1, "real_time_row_period_ms": period_ms,
+            "headroom": period_ms / (dt * 1e3 / n_rows)}
 
 
 def run_e2e(pkg, w, x, mask, xmode, args, torch) -> dict:

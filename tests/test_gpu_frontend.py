@@ -201,3 +201,52 @@ def test_ladder_rows_step_the_phase_slope(pkg, cuda, fe):
             assert abs(r["tau_fit"] - 6 * step) < 0.02, (step, r)
     finally:
         eng.close()
+
+
+def test_front_end_to_files_phase_check(pkg, cuda, fe, tmp_path):
+    """The reference's phase test end to end: synthetic front end -> staging ring ->
+    C ABI rows -> file set -> read the (0,1) baseline file back by the name its
+    metadata gives -> phase slope = injected delay (tools/phase_check.py)."""
+    import os
+    wr = importlib.import_module(pkg.__name__ + ".writer")
+    phase = importlib.import_module(pkg.__name__ + ".phase")
+    n, nf, fps, chunk, slots = 4, 4096, 32, 32, 3
+    n_cum, n_rows = 64, 3                                  # two slots per row
+    tau = 5
+    spec = fe.ReplaySpec(pattern="prng", start_counter=2 * 32 * 4, sample_delay={1: tau},
+                         drop_rate=0.01)
+    cfg = pkg.make_config(n, nf, fps, chunk, slots, 1)
+    names = ["S00", "S01", "S02", "S03"]
+    seq0 = 4                                               # frame 128 = the first full frame
+    with pkg.Correlator(cfg) as c, wr.RowWriter(str(tmp_path), names, nf, n_cum, "h1",
+                                                queue_full="block", frames_per_slot=fps) as w:
+        seq = seq0
+        for r in range(n_rows):
+            valid = np.zeros(n, dtype=np.uint64)
+            for _ in range(n_cum // fps):
+                if seq - seq0 >= slots:
+                    c.row_slot_free(seq - slots)
+                fe.fill_staging(spec, c, seq)
+                for g in range(n):
+                    valid[g] += int(np.unpackbits(c.staging(g).mask[seq % slots],
+                                                  bitorder="little")[:fps].sum())
+                c.row_accumulate(seq, fps)
+                seq += 1
+            c.row_end(n_cum)
+            c.rows_wait()
+            row = c.rows_fetch()[0]
+            w.write_row(row, 1_790_000_000_000 + 1000 * r, r,
+                        (seq0 + r * n_cum // fps) * fps, valid)
+        w.sync()
+        tag = w.stats()["set_tag"]
+    meta = (tmp_path / f"{tag}-metadata.yaml").read_text()
+    line = next(l for l in meta.splitlines() if "j: 0, k: 1," in l)
+    fname = line.split("file: ")[1].rstrip("}")
+    x = np.fromfile(tmp_path / fname, dtype=np.complex64).reshape(-1, nf)
+    assert x.shape[0] == n_rows
+    r = phase.fit_delay(x, 2 * nf, tau)
+    assert abs(r["tau_fit"] - tau) < 0.02 and r["max_resid"] < 0.5, r
+    blocks = (tmp_path / f"{tag}-blocks.csv").read_text().splitlines()
+    assert len(blocks) == n_rows * n
+    assert all(int(b.split(",")[4]) + int(b.split(",")[5]) == n_cum for b in blocks)
+    assert os.path.getsize(tmp_path / f"{tag}-time.bin") == 8 * n_rows
