@@ -213,6 +213,9 @@ def main() -> None:
     ap.add_argument("--tiles", default="",
                     help="XCT,XKT,FPLAN: fixed tensor tile and FFT plan instead of the "
                          "autotuner's (profiling a chosen configuration)")
+    ap.add_argument("--only", default="", choices=["", "frontend", "writer"],
+                    help="run just one side workload (the synthetic front end or the file "
+                         "writer) on this workload's geometry and print its JSON")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the batching and stream workloads")
     args = ap.parse_args()
@@ -221,6 +224,9 @@ def main() -> None:
 
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.only:
+        run_only(args)
         return
 
     import torch
@@ -539,6 +545,24 @@ def run_stream(pkg, synth, torch, stream) -> dict:
             "ms_per_integration": ms, "real_time_factor": gs / need,
             "real_time_need_gsps": need,
             "integrations_per_60s": 60.0 * 250e6 / (w.frames * w.fft_len)}
+
+
+def run_only(args) -> None:
+    """One side workload alone (for profiling it): --only frontend | writer."""
+    import dataclasses
+    pkg = importlib.import_module(PKG_NAME)
+    importlib.import_module(PKG_NAME + ".build").build()
+    synth = importlib.import_module(PKG_NAME + ".synth")
+    w = synth.WORKLOADS[args.workload]
+    if args.frames:
+        w = dataclasses.replace(w, frames=args.frames)
+    if args.only == "writer":
+        print(json.dumps({"writer": run_writer(pkg, w)}), flush=True)
+        return
+    import torch
+    torch.cuda.set_device(0)
+    print(json.dumps({"frontend": run_frontend(pkg, w, torch, torch.cuda.current_stream())}),
+          flush=True)
 
 
 def run_frontend(pkg, w, torch, stream) -> dict:
