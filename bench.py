@@ -216,6 +216,8 @@ def main() -> None:
     ap.add_argument("--only", default="", choices=["", "frontend", "writer"],
                     help="run just one side workload (the synthetic front end or the file "
                          "writer) on this workload's geometry and print its JSON")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the error report against the float64 DFT")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the batching and stream workloads")
     args = ap.parse_args()
@@ -345,6 +347,13 @@ def main() -> None:
                        "tiles": {k: tiles[name][k] for k in ("ytile", "xct", "xkt", "fplan")},
                        "per_vis_err_bound": err_bound[name]}
 
+    # rows of each path for the integration just timed (identical input every step)
+    accuracy = None
+    if rank == 0 and not args.no_accuracy:
+        rows = {name: a_.clone() for name, (e_, a_, s_) in engines.items()}
+        accuracy = accuracy_report(torch, w, x, mask, rows)
+        del rows
+
     # per-kernel times: one pass of PASS_FRAMES frames through each kernel alone
     hbm_peak, _, peak_kind = peaks()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
@@ -436,7 +445,7 @@ def main() -> None:
                        "tiles": paths[best]["tiles"],
                        "frames_per_pass": PASS_FRAMES, "parallelism": f"replicas x{world}",
                        "l2": f"inputs {N * F * L / 1e9:.2f} GB per step > L2; no flush"},
-            "paths": paths, "kernels": kernels, "roofline": roofline,
+            "paths": paths, "kernels": kernels, "roofline": roofline, "accuracy": accuracy,
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
             "gpu_launches": launches_per_step * args.steps,
         }
@@ -537,6 +546,22 @@ def run_stream(pkg, synth, torch, stream) -> dict:
     torch.cuda.synchronize()
     eng.check()
     ms = e0.elapsed_time(e1) / 2
+    # error of the first integration against the float64 DFT at 16 channels
+    acc_rep = accuracy_report(torch, w, x, mask, {"tc_split": acc.clone()})
+    # the F-engine alone on one pass: algorithmic HBM bytes / time
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    lib = eng.lib
+    for r in range(4):
+        ev[0].record(stream)
+        pkg.abi.check(lib.corrx_run_fengine(eng.h, x.data_ptr(), x.stride(0), x.stride(1),
+                                            mask.data_ptr() if mask is not None else None,
+                                            mask.stride(0) if mask is not None else 0, 0,
+                                            PASS_FRAMES, stream.cuda_stream), "fengine")
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+    t_f = ev[0].elapsed_time(ev[1])
+    f_bytes = w.n_station * PASS_FRAMES * (w.fft_len + w.n_freq * 8)
+    hbm, _, kind = peaks()
     eng.close()
     gs = w.n_station * w.frames * w.fft_len / (ms * 1e-3) / 1e9
     need = w.n_station * 0.25
@@ -544,7 +569,71 @@ def run_stream(pkg, synth, torch, stream) -> dict:
             "tiles": {k: tiles[k] for k in ("ytile", "xct", "xkt", "fplan")},
             "ms_per_integration": ms, "real_time_factor": gs / need,
             "real_time_need_gsps": need,
-            "integrations_per_60s": 60.0 * 250e6 / (w.frames * w.fft_len)}
+            "integrations_per_60s": 60.0 * 250e6 / (w.frames * w.fft_len),
+            "fengine": {"ms_per_launch": t_f, "frames_per_launch": PASS_FRAMES,
+                        "achieved_gbs": f_bytes / (t_f * 1e-3) / 1e9,
+                        "frac_of_hbm": f_bytes / (t_f * 1e-3) / 1e9 / hbm, "peak_kind": kind},
+            "accuracy_first_integration": {"channels": acc_rep["channels"],
+                                           "baselines": acc_rep["baselines"],
+                                           "vs_fp64": acc_rep["vs_fp64"]["tc_split"]}}
+
+
+ACCURACY_CHANNELS = [0, 1, 2, 63, 1234, 2047, 3000, 4096, 5555, 8191, 8192, 9000, 12345,
+                     16000, 16382, 16383]
+
+
+def accuracy_report(torch, w, x, mask, rows: dict, channels=ACCURACY_CHANNELS) -> dict:
+    """Errors of each path's rows for one integration (already divided by frames).
+
+    vs_fp64: against an exact float64 DFT of every frame at `channels` (all
+    baselines; lost frames zeroed as the engines do), computed on the device
+    in float64 with matrix products of the int8 frames and the DFT columns.
+    vs_plain: each tensor form against the plain FP32 path over the whole row.
+    rel_rms = ||V - V_ref|| / ||V_ref||; max_per_vis = max |V - V_ref| /
+    sqrt(|V_jj V_kk|) (the error relative to the two inputs' powers).
+    """
+    N, F, L = w.n_station, w.frames, w.fft_len
+    ch = [c for c in channels if c < w.n_freq]
+    dev = x.device
+    t = torch.arange(L, dtype=torch.float64, device=dev)
+    ang = -2.0 * math.pi * torch.outer(t, torch.tensor(ch, dtype=torch.float64, device=dev)) / L
+    Wm = torch.cat([torch.cos(ang), torch.sin(ang)], dim=1)          # [L, 2C]
+    C_ = len(ch)
+    Y = torch.empty((N, F, C_), dtype=torch.complex128, device=dev)
+    step = 512
+    for s_ in range(N):
+        for f0 in range(0, F, step):
+            blk = x[s_, f0:f0 + step].to(torch.float64)
+            if mask is not None:
+                fr = torch.arange(f0, min(f0 + step, F), device=dev)
+                bits = (mask[s_, fr // 8].to(torch.int64) >> (fr % 8)) & 1
+                blk = blk * bits.to(torch.float64)[:, None]
+            prod = blk @ Wm
+            Y[s_, f0:f0 + step] = torch.complex(prod[:, :C_], prod[:, C_:])
+    pairs = [(j, k) for j in range(N) for k in range(j, N)]
+    jj = torch.tensor([p[0] for p in pairs], device=dev)
+    kk = torch.tensor([p[1] for p in pairs], device=dev)
+    ref = torch.einsum("bfc,bfc->bc", Y[jj], Y[kk].conj()) / F              # [B, C]
+    auto_idx = torch.tensor([pairs.index((i, i)) for i in range(N)], device=dev)
+
+    def errs(got, want):
+        d = (got - want).abs()
+        rel_rms = float(torch.linalg.vector_norm(got - want) / torch.linalg.vector_norm(want))
+        autos = want[auto_idx].real.abs()                                    # [N, C]
+        norm = torch.sqrt(autos[jj] * autos[kk])
+        return {"rel_rms": rel_rms, "max_per_vis": float((d / norm).max())}
+
+    chi = torch.tensor(ch, device=dev)
+    out = {"channels": ch, "baselines": len(pairs), "frames": F, "vs_fp64": {}, "vs_plain": {}}
+    for name, r in rows.items():
+        out["vs_fp64"][name] = errs(r[:, chi].to(torch.complex128), ref)
+    if "plain" in rows:
+        p_ = rows["plain"].to(torch.complex128)
+        for name, r in rows.items():
+            if name != "plain":
+                out["vs_plain"][name] = errs(r.to(torch.complex128), p_)
+    del Y
+    return out
 
 
 def run_only(args) -> None:
