@@ -590,7 +590,9 @@ def accuracy_report(torch, w, x, mask, rows: dict, channels=ACCURACY_CHANNELS) -
     in float64 with matrix products of the int8 frames and the DFT columns.
     vs_plain: each tensor form against the plain FP32 path over the whole row.
     rel_rms = ||V - V_ref|| / ||V_ref||; max_per_vis = max |V - V_ref| /
-    sqrt(|V_jj V_kk|) (the error relative to the two inputs' powers).
+    sqrt(|V_jj V_kk|) (the error relative to the two inputs' powers);
+    elementwise_max / _rms = |V - V_ref| / |V_ref| over the visibilities with
+    |V_ref| > 1e-3 sqrt(|V_jj V_kk|) (near-zero cross terms excluded).
     """
     N, F, L = w.n_station, w.frames, w.fft_len
     ch = [c for c in channels if c < w.n_freq]
@@ -621,7 +623,13 @@ def accuracy_report(torch, w, x, mask, rows: dict, channels=ACCURACY_CHANNELS) -
         rel_rms = float(torch.linalg.vector_norm(got - want) / torch.linalg.vector_norm(want))
         autos = want[auto_idx].real.abs()                                    # [N, C]
         norm = torch.sqrt(autos[jj] * autos[kk])
-        return {"rel_rms": rel_rms, "max_per_vis": float((d / norm).max())}
+        # elementwise relative error where the visibility is not near zero
+        big = want.abs() > 1e-3 * norm
+        rel = d[big] / want.abs()[big]
+        return {"rel_rms": rel_rms, "max_per_vis": float((d / norm).max()),
+                "elementwise_max": float(rel.max()),
+                "elementwise_rms": float(torch.sqrt((rel ** 2).mean())),
+                "elementwise_count": int(big.sum())}
 
     chi = torch.tensor(ch, device=dev)
     out = {"channels": ch, "baselines": len(pairs), "frames": F, "vs_fp64": {}, "vs_plain": {}}
