@@ -182,7 +182,8 @@ TcGeom make_geom(int n_station, bool split, int ct, int kt) {
     const int slack = std::max(0, reach - g.region_stride) + 7 * 16 + 128;
     g.op_stage = round_up(g.regions * g.region_stride + slack, 128);
     g.ld_stage = kt * N * ct * g.elem;
-    g.items = ct * N * (kt / 8);
+    // paired form: items enumerate stations in groups of four (see the converters)
+    g.items = ct * (g.form == kFp16Paired ? round_up(N, 4) : N) * (kt / 8);
     if (g.items > kMaxItems * kConverters) return g;
     const int n_baseline = N * (N + 1) / 2;
     g.vs_bytes = round_up(n_baseline * ct * 8, 128);
@@ -447,6 +448,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         // This thread's items (channel c, station s, 8-frame group kq) are the
         // same every stage: keep their fp32 and operand offsets.
         int n_item = 0;
+        uint32_t item_ok = 0;                   // bit i: item i exists (station groups may be short)
         uint32_t it_ld[kMaxItems], it_op[kMaxItems];
         const int lo_off = (g.R / 8) * g.sbo;   // Dl rows start at row R
 #pragma unroll
@@ -454,11 +456,31 @@ __global__ void __launch_bounds__(kThreads, 1)
             it_ld[i] = 0;
             it_op[i] = 0;
             const int q = wt + i * kConverters;
-            if (q < g.items) {
-                const int c = q % g.ct;
+            int c, s, kq;
+            if (g.form == kFp16Paired) {
+                // A quarter warp (whose 16-byte stores share one bank line) takes
+                // every region x four consecutive stations of one channel half.
+                // Rows 2s of four stations fall in four distinct 16-byte slots and
+                // the region skew separates the regions; the two halves of a
+                // region are R = 64 rows = 8 row groups apart, the same slot, so
+                // they go to different quarter warps.
+                const int regions = g.ct / 2;
+                int rest = q / regions;
+                const int s_lo = rest % 4;
+                rest /= 4;
+                const int half = rest % 2;
+                rest /= 2;
+                const int groups = (N + 3) / 4;
+                s = (rest % groups) * 4 + s_lo;
+                kq = rest / groups;
+                c = (q % regions) * 2 + half;
+            } else {
+                c = q % g.ct;
                 const int rest = q / g.ct;
-                const int s = rest % N;
-                const int kq = rest / N;
+                s = rest % N;
+                kq = rest / N;
+            }
+            if (q < g.items && s < N) {
                 int region = c, row = 2 * s;
                 if (g.form == kFp16Paired) {
                     region = c >> 1;
@@ -468,6 +490,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 it_op[i] = static_cast<uint32_t>(region * g.region_stride + region_skew(region) +
                                                  (row >> 3) * g.sbo + kq * kLBO + (row & 7) * 16);
                 n_item = i + 1;
+                item_ok |= 1u << i;
             }
         }
         const int row_step = N * g.ct;   // float2 between consecutive frames of a slot
@@ -494,6 +517,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                 for (int it = 0; it < kMaxItems; ++it) {
                     if (it >= n_item) break;
+                    if (!((item_ok >> it) & 1u)) continue;
                     const uint32_t *src = ld16 + it_ld[it];
                     uint32_t hre[4], him[4];
 #pragma unroll
@@ -515,6 +539,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                 for (int it = 0; it < kMaxItems; ++it) {
                     if (it >= n_item) break;
+                    if (!((item_ok >> it) & 1u)) continue;
                     const uint2 *src = ld2 + it_ld[it];
                     uint32_t hre[4], him[4], lre[4], lim[4];
 #pragma unroll
