@@ -333,14 +333,14 @@ corr_status fxplan_set_tiles(FxPlan *p, int ytile, int xct, int xkt, int fplan) 
             return failf(CORR_ERR_ARG,
                          "no tensor X-engine tile of %d channels x %d frames for %d inputs", xct,
                          xkt, p->n_station);
-        if (ytile < xct)
-            return failf(CORR_ERR_ARG, "ytile=%d is narrower than the tensor tile (%d channels)",
-                         ytile, xct);
-        if (ytile != p->n_freq)
+        // The tensor forms read either contiguous rows (a TMA tile per stage)
+        // or tiles of exactly their own width, where a stage is one contiguous
+        // block (a single bulk copy per stage).
+        if (ytile != p->n_freq && ytile != xct)
             return failf(CORR_ERR_ARG,
-                         "the tensor X-engines read FP16 spectra written as contiguous rows: "
-                         "ytile must be n_freq=%d",
-                         p->n_freq);
+                         "the tensor X-engines read contiguous rows (ytile = n_freq = %d) or "
+                         "tiles of their own width (ytile = xct = %d), not ytile = %d",
+                         p->n_freq, xct, ytile);
         p->xct = xct;
         p->xkt = xkt;
     }
@@ -362,8 +362,10 @@ corr_status fxplan_autotune(FxPlan *p, cudaStream_t stream, corrx_tiles *out) {
         const bool split = p->xmode == CORR_X_TC_FP16_SPLIT;
         for (int ct = 8; ct >= 2; ct /= 2)
             for (int kt = 16; kt <= 64; kt *= 2)
-                if (xengine_tc_shape_ok(p->n_station, split, ct, kt))
+                if (xengine_tc_shape_ok(p->n_station, split, ct, kt)) {
                     cands.push_back({p->n_freq, ct, kt});
+                    if (ct < p->n_freq) cands.push_back({ct, ct, kt});
+                }
     }
     if (cands.empty()) return fail(CORR_ERR_INTERNAL, "autotune: no candidate tile");
     const int frames = std::min(p->max_frames, 1024);
@@ -413,16 +415,17 @@ corr_status fxplan_autotune(FxPlan *p, cudaStream_t stream, corrx_tiles *out) {
                                  stream);
     };
     auto run_x = [&] { return corrx_run_xengine(p, frames, d_acc, stream); };
-    // The F-engine's time depends on the layout and the FFT plan, the
-    // X-engine's on the layout and the tile: time each pair once.
+    // The F-engine's time depends on the FFT plan and the spectra layout, the
+    // X-engine's on the layout and the tile. The plan is chosen on contiguous
+    // rows; then every (layout, tile) is timed, the F-engine once per layout,
+    // and the pair with the smallest F + X time wins.
     const int fplan0 = p->fplan;
     const int n_fplans = fengine_plans(p->n_freq);
-    float best_f = 1e30f, best_x = 1e30f;
+    float best_f = 1e30f, best_x = 1e30f, best_sum = 1e30f;
     int best_fplan = fplan0;
     Cand best{ytile0, ct0, kt0};
-    const int ytile = p->n_freq;   // every candidate uses contiguous rows
     for (int fp = 0; fp < n_fplans && st == CORR_OK; ++fp) {
-        if ((st = fxplan_set_tiles(p, ytile, cands[0].ct, cands[0].kt, fp)) != CORR_OK) break;
+        if ((st = fxplan_set_tiles(p, p->n_freq, cands[0].ct, cands[0].kt, fp)) != CORR_OK) break;
         float f_ms = 0.f;
         if ((st = timed(run_f, &f_ms)) != CORR_OK) break;
         if (f_ms < best_f) {
@@ -430,14 +433,25 @@ corr_status fxplan_autotune(FxPlan *p, cudaStream_t stream, corrx_tiles *out) {
             best_fplan = fp;
         }
     }
+    std::vector<std::pair<int, float>> f_by_layout;   // ytile -> F-engine ms
     for (const Cand &c : cands) {
         if (st != CORR_OK) break;
         if (fxplan_set_tiles(p, c.ytile, c.ct, c.kt, best_fplan) != CORR_OK)
             continue;   // not for this form
-        if ((st = run_f()) != CORR_OK) break;   // the spectra this form reads
+        float f_ms = -1.f;
+        for (const auto &e : f_by_layout)
+            if (e.first == c.ytile) f_ms = e.second;
+        if (f_ms < 0.f) {
+            if ((st = timed(run_f, &f_ms)) != CORR_OK) break;
+            f_by_layout.emplace_back(c.ytile, f_ms);
+        } else if ((st = run_f()) != CORR_OK) {   // the spectra this layout holds
+            break;
+        }
         float x_ms = 0.f;
         if ((st = timed(run_x, &x_ms)) != CORR_OK) break;
-        if (x_ms < best_x) {
+        if (f_ms + x_ms < best_sum) {
+            best_sum = f_ms + x_ms;
+            best_f = f_ms;
             best_x = x_ms;
             best = c;
         }

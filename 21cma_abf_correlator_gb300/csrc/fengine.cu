@@ -543,12 +543,12 @@ template <int LOGM, int PLAN>
 corr_status launch_plan(const FengineArgs &a, const TwiddleTables &tw, int num_sms,
                         cudaStream_t stream) {
     const bool contig = a.ytile == (1 << LOGM);
-    if (a.y_fmt != kSpectraF32) {
-        if (!contig)
-            return fail(CORR_ERR_ARG, "FP16 spectra are written as contiguous rows (ytile = n_freq)");
-        if (a.y_fmt == kSpectraF16) return launch_one<LOGM, PLAN, kSpectraF16, true>(a, tw, num_sms, stream);
-        return launch_one<LOGM, PLAN, kSpectraF16Split, true>(a, tw, num_sms, stream);
-    }
+    if (a.y_fmt == kSpectraF16)
+        return contig ? launch_one<LOGM, PLAN, kSpectraF16, true>(a, tw, num_sms, stream)
+                      : launch_one<LOGM, PLAN, kSpectraF16, false>(a, tw, num_sms, stream);
+    if (a.y_fmt == kSpectraF16Split)
+        return contig ? launch_one<LOGM, PLAN, kSpectraF16Split, true>(a, tw, num_sms, stream)
+                      : launch_one<LOGM, PLAN, kSpectraF16Split, false>(a, tw, num_sms, stream);
     if (contig) return launch_one<LOGM, PLAN, kSpectraF32, true>(a, tw, num_sms, stream);
     return launch_one<LOGM, PLAN, kSpectraF32, false>(a, tw, num_sms, stream);
 }

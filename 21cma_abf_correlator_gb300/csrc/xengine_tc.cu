@@ -59,6 +59,7 @@
 
 #include <algorithm>
 #include <mutex>
+#include <type_traits>
 
 #include <cuda.h>
 #include <cuda_fp16.h>
@@ -274,6 +275,9 @@ __device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, i
 
 struct TcParams {
     int ytile;
+    int bulk;          // ytile == CT: a stage is one contiguous block, loaded by one bulk copy
+    const unsigned char *y;   // spectra (bulk loads)
+    int y_frames;      // frames per spectra tile (bulk loads)
     int in_fmt;        // SpectraFormat: FP16 pairs, or FP16 hi/lo pairs (already scaled)
     int n_station;
     int n_freq;
@@ -388,10 +392,25 @@ __global__ void __launch_bounds__(kThreads, 1)
                     break;
                 }
                 const int c0 = tile_c0(tl);
-                mbar_arrive_expect_tx(&bars.load_full[slot], static_cast<uint32_t>(g.ld_stage));
-                // frames past `frames` (the map's last frame) arrive as zeros
-                tma_load_4d(ld_ring + slot * g.ld_stage, &ymap, c0 & (p.ytile - 1), 0,
-                            st * g.kt, c0 / p.ytile, &bars.load_full[slot]);
+                if (p.bulk) {
+                    // channel tiles of CT bins: the stage's frames x stations x CT
+                    // bins are contiguous. Only the launch's frames are copied; the
+                    // converters treat the rest of a last, partial stage as zeros.
+                    const int f0 = st * g.kt;
+                    const int nf = min(g.kt, p.frames - f0);
+                    const uint32_t row = static_cast<uint32_t>(N * g.ct * g.elem);
+                    const unsigned char *src =
+                        p.y + (static_cast<size_t>(c0 / g.ct) * p.y_frames + f0) * row;
+                    mbar_arrive_expect_tx(&bars.load_full[slot], nf * row);
+                    bulk_copy_g2s(ld_ring + slot * g.ld_stage, src, nf * row,
+                                  &bars.load_full[slot]);
+                } else {
+                    mbar_arrive_expect_tx(&bars.load_full[slot],
+                                          static_cast<uint32_t>(g.ld_stage));
+                    // frames past `frames` (the map's last frame) arrive as zeros
+                    tma_load_4d(ld_ring + slot * g.ld_stage, &ymap, c0 & (p.ytile - 1), 0,
+                                st * g.kt, c0 / p.ytile, &bars.load_full[slot]);
+                }
                 ++s_ld_issued;
             }
         }
@@ -450,11 +469,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         int n_item = 0;
         uint32_t item_ok = 0;                   // bit i: item i exists (station groups may be short)
         uint32_t it_ld[kMaxItems], it_op[kMaxItems];
+        int it_f0[kMaxItems];                   // first frame of the item's 8-frame group
         const int lo_off = (g.R / 8) * g.sbo;   // Dl rows start at row R
 #pragma unroll
         for (int i = 0; i < kMaxItems; ++i) {
             it_ld[i] = 0;
             it_op[i] = 0;
+            it_f0[i] = 0;
             const int q = wt + i * kConverters;
             int c, s, kq;
             if (g.form == kFp16Paired) {
@@ -489,6 +510,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 it_ld[i] = static_cast<uint32_t>((kq * 8 * N + s) * g.ct + c);
                 it_op[i] = static_cast<uint32_t>(region * g.region_stride + region_skew(region) +
                                                  (row >> 3) * g.sbo + kq * kLBO + (row & 7) * 16);
+                it_f0[i] = kq * 8;
                 n_item = i + 1;
                 item_ok |= 1u << i;
             }
@@ -510,57 +532,73 @@ __global__ void __launch_bounds__(kThreads, 1)
             // spectra slot: [frame][station][CT channels]
             const float2 *ld = reinterpret_cast<const float2 *>(ld_ring + lb * g.ld_stage);
             unsigned char *op = op_ring + ob * g.op_stage;
-            if (p.in_fmt == kSpectraF16) {
-                // FP16 pairs (re, im) per frame: regroup into 8-frame rows of re
-                // and of im, two byte-permutes per frame pair
-                const uint32_t *ld16 = reinterpret_cast<const uint32_t *>(ld);
+            // Frames of a bulk-loaded last stage past the launch's frames were not
+            // copied (stale bytes): they convert as zeros. A tensor-map load
+            // zero-fills them itself.
+            const int st_here = gs % n_stages;
+            const int n_valid = p.bulk ? min(g.kt, p.frames - st_here * g.kt) : g.kt;
+            auto convert = [&](auto guard_tag) {
+                constexpr bool kGuard = decltype(guard_tag)::value;
+                if (p.in_fmt == kSpectraF16) {
+                    // FP16 pairs (re, im) per frame: regroup into 8-frame rows of re
+                    // and of im, two byte-permutes per frame pair
+                    const uint32_t *ld16 = reinterpret_cast<const uint32_t *>(ld);
 #pragma unroll
-                for (int it = 0; it < kMaxItems; ++it) {
-                    if (it >= n_item) break;
-                    if (!((item_ok >> it) & 1u)) continue;
-                    const uint32_t *src = ld16 + it_ld[it];
-                    uint32_t hre[4], him[4];
+                    for (int it = 0; it < kMaxItems; ++it) {
+                        if (it >= n_item) break;
+                        if (!((item_ok >> it) & 1u)) continue;
+                        const uint32_t *src = ld16 + it_ld[it];
+                        uint32_t hre[4], him[4];
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const uint32_t w0 = src[(2 * i) * row_step];
-                        const uint32_t w1 = src[(2 * i + 1) * row_step];
-                        hre[i] = __byte_perm(w0, w1, 0x5410);
-                        him[i] = __byte_perm(w0, w1, 0x7632);
+                        for (int i = 0; i < 4; ++i) {
+                            uint32_t w0 = 0, w1 = 0;
+                            if (!kGuard || it_f0[it] + 2 * i < n_valid) w0 = src[(2 * i) * row_step];
+                            if (!kGuard || it_f0[it] + 2 * i + 1 < n_valid)
+                                w1 = src[(2 * i + 1) * row_step];
+                            hre[i] = __byte_perm(w0, w1, 0x5410);
+                            him[i] = __byte_perm(w0, w1, 0x7632);
+                        }
+                        unsigned char *dst = op + it_op[it];
+                        *reinterpret_cast<uint4 *>(dst) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
+                        *reinterpret_cast<uint4 *>(dst + 16) =
+                            make_uint4(him[0], him[1], him[2], him[3]);
                     }
-                    unsigned char *dst = op + it_op[it];
-                    *reinterpret_cast<uint4 *>(dst) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
-                    *reinterpret_cast<uint4 *>(dst + 16) =
-                        make_uint4(him[0], him[1], him[2], him[3]);
-                }
-            } else {
-                // FP16 hi/lo pairs per frame: the Dh rows from the h words, the Dl
-                // rows from the l words
-                const uint2 *ld2 = reinterpret_cast<const uint2 *>(ld);
+                } else {
+                    // FP16 hi/lo pairs per frame: the Dh rows from the h words, the
+                    // Dl rows from the l words
+                    const uint2 *ld2 = reinterpret_cast<const uint2 *>(ld);
 #pragma unroll
-                for (int it = 0; it < kMaxItems; ++it) {
-                    if (it >= n_item) break;
-                    if (!((item_ok >> it) & 1u)) continue;
-                    const uint2 *src = ld2 + it_ld[it];
-                    uint32_t hre[4], him[4], lre[4], lim[4];
+                    for (int it = 0; it < kMaxItems; ++it) {
+                        if (it >= n_item) break;
+                        if (!((item_ok >> it) & 1u)) continue;
+                        const uint2 *src = ld2 + it_ld[it];
+                        uint32_t hre[4], him[4], lre[4], lim[4];
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const uint2 w0 = src[(2 * i) * row_step];
-                        const uint2 w1 = src[(2 * i + 1) * row_step];
-                        hre[i] = __byte_perm(w0.x, w1.x, 0x5410);
-                        him[i] = __byte_perm(w0.x, w1.x, 0x7632);
-                        lre[i] = __byte_perm(w0.y, w1.y, 0x5410);
-                        lim[i] = __byte_perm(w0.y, w1.y, 0x7632);
+                        for (int i = 0; i < 4; ++i) {
+                            uint2 w0 = make_uint2(0u, 0u), w1 = make_uint2(0u, 0u);
+                            if (!kGuard || it_f0[it] + 2 * i < n_valid) w0 = src[(2 * i) * row_step];
+                            if (!kGuard || it_f0[it] + 2 * i + 1 < n_valid)
+                                w1 = src[(2 * i + 1) * row_step];
+                            hre[i] = __byte_perm(w0.x, w1.x, 0x5410);
+                            him[i] = __byte_perm(w0.x, w1.x, 0x7632);
+                            lre[i] = __byte_perm(w0.y, w1.y, 0x5410);
+                            lim[i] = __byte_perm(w0.y, w1.y, 0x7632);
+                        }
+                        unsigned char *dst = op + it_op[it];
+                        *reinterpret_cast<uint4 *>(dst) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
+                        *reinterpret_cast<uint4 *>(dst + 16) =
+                            make_uint4(him[0], him[1], him[2], him[3]);
+                        *reinterpret_cast<uint4 *>(dst + lo_off) =
+                            make_uint4(lre[0], lre[1], lre[2], lre[3]);
+                        *reinterpret_cast<uint4 *>(dst + lo_off + 16) =
+                            make_uint4(lim[0], lim[1], lim[2], lim[3]);
                     }
-                    unsigned char *dst = op + it_op[it];
-                    *reinterpret_cast<uint4 *>(dst) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
-                    *reinterpret_cast<uint4 *>(dst + 16) =
-                        make_uint4(him[0], him[1], him[2], him[3]);
-                    *reinterpret_cast<uint4 *>(dst + lo_off) =
-                        make_uint4(lre[0], lre[1], lre[2], lre[3]);
-                    *reinterpret_cast<uint4 *>(dst + lo_off + 16) =
-                        make_uint4(lim[0], lim[1], lim[2], lim[3]);
                 }
-            }
+            };
+            if (n_valid == g.kt)
+                convert(std::false_type{});
+            else
+                convert(std::true_type{});
             mbar_arrive(&bars.load_empty[lb]);   // the spectra slot may be refilled
             fence_proxy_async_smem();   // operand stores -> visible to the tensor cores
             mbar_arrive(&bars.op_full[ob]);
@@ -832,6 +870,11 @@ corr_status xengine_tc_launch(const XengineArgs &a, bool split, int ct, int kt, 
     }
     TcParams p{};
     p.ytile = a.ytile;
+    p.bulk = a.ytile == g.ct;
+    p.y = reinterpret_cast<const unsigned char *>(a.y);
+    p.y_frames = a.y_frames;
+    if (p.bulk && (reinterpret_cast<uintptr_t>(a.y) & 15) != 0)
+        return fail(CORR_ERR_INTERNAL, "spectra buffer is not 16-byte aligned");
     p.in_fmt = a.y_fmt;
     p.n_station = a.n_station;
     p.n_freq = a.n_freq;

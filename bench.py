@@ -211,8 +211,9 @@ def main() -> None:
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the default tile shapes instead of autotuning them")
     ap.add_argument("--tiles", default="",
-                    help="XCT,XKT,FPLAN: fixed tensor tile and FFT plan instead of the "
-                         "autotuner's (profiling a chosen configuration)")
+                    help="XCT,XKT,FPLAN[,YTILE]: fixed tensor tile, FFT plan and spectra "
+                         "layout (default n_freq) instead of the autotuner's (profiling a "
+                         "chosen configuration)")
     ap.add_argument("--only", default="", choices=["", "frontend", "writer"],
                     help="run just one side workload (the synthetic front end or the file "
                          "writer) on this workload's geometry and print its JSON")
@@ -283,8 +284,9 @@ def main() -> None:
         try:
             eng = pkg.FxEngine(N, nf, PASS_FRAMES, xmode=modes[name])
             if args.tiles:
-                xct, xkt, fplan = (int(v) for v in args.tiles.split(","))
-                eng.set_tiles(nf, xct, xkt, fplan)
+                vals = [int(v) for v in args.tiles.split(",")]
+                xct, xkt, fplan = vals[:3]
+                eng.set_tiles(vals[3] if len(vals) > 3 else nf, xct, xkt, fplan)
                 tiles[name] = eng.tiles()
             elif args.no_tune:
                 tiles[name] = eng.tiles()
