@@ -74,13 +74,12 @@ corr_status corrx_check(void *eng);
 /*
  * Tile shapes of an engine. ytile is the spectra layout between the F- and
  * X-engines: n_freq = one contiguous row per (frame, station); a smaller power
- * of two = channel tiles of that width holding every frame and station (plain
- * X-engine only: the tensor forms read FP16 spectra written as contiguous rows).
- * xct and
- * xkt are the tensor X-engine's channels per CTA tile (2, 4, 8) and frames per
- * pipeline stage (16, 32, 64); the plain X-engine ignores them. corrx_create
- * picks contiguous rows and the widest feasible tensor tile with 32-frame stages
- * (16 if none fits).
+ * of two = channel tiles of that width holding every frame and station (any
+ * width for the plain X-engine; for the tensor forms only ytile = xct, where a
+ * stage is one contiguous block). xct and xkt are the tensor X-engine's
+ * channels per CTA tile (2, 4, 8) and frames per pipeline stage (16, 32, 64);
+ * the plain X-engine ignores them. corrx_create picks contiguous rows and the
+ * widest feasible tensor tile with 32-frame stages (16 if none fits).
  */
 typedef struct corrx_tiles {
     uint32_t struct_size; /* sizeof(corrx_tiles)                                   */
