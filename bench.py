@@ -463,10 +463,10 @@ def main() -> None:
 # traffic is all per frame (int8 read, spectra write); the X-engines' is the
 # spectra read (per frame) plus the row's read and write (per launch).
 _NCU_256 = {
-    "fengine": {"tc": (543.183616e6, 0.0), "tc_split": (944.986112e6, 0.0),
-                "plain": (945.010432e6, 0.0)},
-    "xengine": {"tc": (402.653184e6, 69.404160e6), "tc_split": (805.306368e6, 74.243584e6),
-                "plain": (805.306368e6, 73.059328e6)},
+    "fengine": {"tc": (543.339520e6, 0.0), "tc_split": (944.290816e6, 0.0),
+                "plain": (944.951296e6, 0.0)},
+    "xengine": {"tc": (402.653184e6, 69.594368e6), "tc_split": (805.306368e6, 74.313728e6),
+                "plain": (805.306368e6, 73.831936e6)},
 }
 
 
