@@ -737,7 +737,7 @@ def run_e2e(pkg, w, x, mask, xmode, args, torch) -> dict:
     cfg = pkg.make_config(N, w.n_freq, fps, fps, block_slots, 1)
     c = pkg.Correlator(cfg)
     c.set_xengine(xmode)
-    c.autotune()
+    tiles = c.autotune() if not args.no_tune else None
     # fill the ring once from the device-resident inputs (receive side's job)
     host = x[:, : fps * block_slots].cpu().numpy()
     for g in range(N):
@@ -765,11 +765,16 @@ def run_e2e(pkg, w, x, mask, xmode, args, torch) -> dict:
 
     for _ in range(2):
         integration()
-    t0 = time.perf_counter()
+    # wall clock on the host: the median of three rounds, so that one hiccup of
+    # the host's scheduler does not stand for the path
     k = max(2, args.steps // 2)
-    for _ in range(k):
-        integration()
-    dt = (time.perf_counter() - t0) / k
+    rounds = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        for _ in range(k):
+            integration()
+        rounds.append((time.perf_counter() - t0) / k)
+    dt = statistics.median(rounds)
     for s in range(seq[0] - 1, max(seq[0] - block_slots, 0) - 1, -1):
         c.row_slot_free(s)
     c.lib.corr_host_free(pinned)
@@ -779,7 +784,9 @@ def run_e2e(pkg, w, x, mask, xmode, args, torch) -> dict:
     d2h = w.n_baseline * w.n_freq * 8
     return {"value": N * F * L / dt / 1e9, "unit": "GSample/s", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "ms_per_step": dt * 1e3, "steps": k,
-            "path": "corr_row_accumulate/row_end/rows_fetch from pinned staging"}
+            "rounds_ms": [r * 1e3 for r in rounds],
+            "path": "corr_row_accumulate/row_end/rows_fetch from pinned staging",
+            "tiles": tiles}
 
 
 if __name__ == "__main__":
