@@ -357,7 +357,7 @@ extern "C" corr_status corr_create(const corr_config *cfg, void **out_ctx) {
     }
     if (devices.size() > 1)
         return failf(CORR_ERR_NOT_IMPL,
-                     "n_devices=%zu: this build drives one GPU per context; run one context "
+                     "n_devices=%zu: this library drives one GPU per context; run one context "
                      "per device and add the rows on the host",
                      devices.size());
 

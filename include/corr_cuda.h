@@ -43,7 +43,7 @@ extern "C" {
    device and cleared by corr_row_slot_free() (corr_cuda.h:94 in the reference). */
 #define CORR_ABI_VERSION 7u
 
-/* Split modes (reference corr_cuda.h:113-137). This build runs one device, on
+/* Split modes (reference corr_cuda.h:113-137). This library runs one device, on
    which all three describe the same placement: every station, every baseline. */
 #define CORR_SPLIT_BASELINE_RANGE 0
 #define CORR_SPLIT_PAIR_COVERING 1
@@ -63,7 +63,7 @@ typedef enum corr_status {
     CORR_ERR_STATE    = 5, /* call out of order for this context or slot */
     CORR_ERR_BUSY     = 6, /* slot or row stack still owned by the GPU   */
     CORR_ERR_NOMEM    = 7, /* host or device allocation failed           */
-    CORR_ERR_NOT_IMPL = 8, /* not supported by this build                */
+    CORR_ERR_NOT_IMPL = 8, /* not supported by this library              */
     CORR_ERR_INTERNAL = 9  /* device-side watchdog or invariant failure  */
 } corr_status;
 
@@ -82,7 +82,7 @@ typedef enum corr_status {
  *   frames_per_slot >= 1, 1 <= chunk_frames <= frames_per_slot
  *   block_slots >= 2, rows_per_fetch >= 1
  *   the device ordinal(s) exist and are distinct; more than one device is
- *       CORR_ERR_NOT_IMPL in this build
+ *       CORR_ERR_NOT_IMPL in this library
  */
 typedef struct corr_config {
     uint32_t abi_version;
