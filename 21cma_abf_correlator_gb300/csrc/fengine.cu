@@ -12,16 +12,16 @@
 //     as zeros, which is what zeroing the samples and transforming them gives;
 //   * the real frame x[0..L) (L = 2M) is packed as M complex points
 //     z[n] = x[2n] + i*x[2n+1] and transformed by a Stockham autosort FFT in
-//     shared memory (radix-16 passes, one final radix-2/4/8 pass), FP32 in
-//     registers, twiddles from host-computed double-precision tables;
+//     shared memory (three or four passes of radix 8..32, FePlan below), FP32
+//     in registers, twiddles from host-computed double-precision tables;
 //   * the split X[k] = Fe[k] + w^k Fo[k] turns Z into the L-point real spectrum;
 //     bins 0..M-1 are written, the Nyquist bin M is dropped and nothing is
 //     normalised (reference semantics, HANDOFF.md:583-602).
 //
-// Output layout (engine.h, y_index): complex64 in channel tiles of `ytile`
-// bins; bin k of (frame f, station s) lands at
-// ((k/ytile)*y_frames + f)*n_station + s)*ytile + k%ytile. The fused last pass
-// writes 32 consecutive bins per warp store: whole pieces of ytile*8 bytes.
+// Output layout (engine.h, y_index): bins in channel tiles of `ytile`; bin k of
+// (frame f, station s) lands at ((k/ytile)*y_frames + f)*n_station + s)*ytile +
+// k%ytile, as FP32 pairs, FP16 pairs or FP16 hi/lo pairs (YRow). The fused last
+// pass writes 32 consecutive bins per warp store.
 
 #include <cmath>
 #include <type_traits>
