@@ -40,11 +40,12 @@
 // stage's DRAM time.
 //
 // Warp-specialised persistent CTAs, one per SM (TMEM), CT channels per tile:
-//   warp 0 (lane 0): TMA tensor loads -- one 4-D box {CT channels, N stations,
-//     KT frames, 1 tile} of the spectra per stage into a ring as deep as shared
-//     memory allows.
-//     The map ends at the launch's last frame, so a partial stage arrives
-//     zero-padded.
+//   warp 0 (lane 0): stage loads into a ring as deep as shared memory allows.
+//     Contiguous rows (ytile = n_freq): one 4-D TMA box {CT channels, N
+//     stations, KT frames, 1 tile} per stage; the map ends at the launch's last
+//     frame, so a partial stage arrives zero-padded. Tiles of CT channels
+//     (ytile = CT): the stage is one contiguous block and one bulk copy brings
+//     the launch's frames of it; the converters read the rest as zeros.
 //   warps 1..kIssuers (lane 0): the MMAs of a stage once its operands are
 //     written, the operand regions dealt round robin over the issuers.
 //   converter warps: regroup a landed stage (FP16 bins, frame-major) into the
