@@ -158,7 +158,8 @@ def time_cpu_oracle(w, target_s: float, processes: int) -> dict:
     return {"value": samples / wall / 1e9, "unit": "GSample/s", "cores": processes,
             "sample": f"{frames_per_proc * processes} frames x {w.n_station} inputs x {L} samples "
                       f"({w.name}), numpy float64 rfft + per-baseline sum, "
-                      f"{processes} process(es), {wall:.1f} s wall"}
+                      f"{processes} process(es) of one thread each (pocketfft, einsum), "
+                      f"{wall:.1f} s wall"}
 
 
 def run_reference(args) -> None:
