@@ -26,7 +26,7 @@ from pathlib import Path
 
 import numpy as np
 
-PKG = __name__.rsplit(".", 1)[0]
+PKG = __package__ or __name__.rsplit(".", 1)[0]
 
 
 def run(directory: str, n_station: int = 8, n_freq: int = 4096, frames_per_slot: int = 64,
