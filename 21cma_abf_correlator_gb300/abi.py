@@ -137,6 +137,14 @@ class corrx_frontend(C.Structure):
     ]
 
 
+class corrx_tc_geom(C.Structure):
+    """The tensor X-engine's geometry for one tile shape (corrx_tc_geometry)."""
+    _fields_ = [("struct_size", C.c_uint32)] + [
+        (n, C.c_int32) for n in ("ok", "form", "elem", "R", "nb", "regions", "sbo",
+                                 "region_stride", "op_stage", "ld_stage", "n_op", "n_ld",
+                                 "acc_cols", "n_acc", "tmem_cols", "items", "smem")]
+
+
 CORRW_SET_AUTO, CORRW_SET_NEW, CORRW_SET_EXPLICIT = 0, 1, 2
 CORRW_QUEUE_DROP, CORRW_QUEUE_BLOCK = 0, 1
 
@@ -262,6 +270,8 @@ SIGNATURES = {
     "corrx_frontend_fill": (C.c_int, [C.POINTER(corrx_frontend), C.c_int32, C.c_int32,
                                       C.c_int32, C.c_int64, C.c_int32, C.c_void_p, C.c_size_t, C.c_size_t,
                                       C.c_void_p, C.c_size_t, C.c_void_p]),
+    "corrx_tc_geometry": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                    C.POINTER(corrx_tc_geom)]),
     "corrw_open": (C.c_int, [C.POINTER(corrw_params), C.POINTER(C.c_void_p),
                              C.POINTER(corrw_resume)]),
     "corrw_write_row": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int64, C.c_uint64,

@@ -800,6 +800,42 @@ bool xengine_tc_shape_ok(int n_station, bool split, int ct, int kt) {
     return make_geom(n_station, split, ct, kt).ok;
 }
 
+} // namespace corrgb
+
+extern "C" corr_status corrx_tc_geometry(int32_t n_station, int32_t split, int32_t ct,
+                                         int32_t kt, corrx_tc_geom *out) {
+    using namespace corrgb;
+    if (out == nullptr) return fail(CORR_ERR_ARG, "out must not be NULL");
+    if (out->struct_size != sizeof(corrx_tc_geom))
+        return failf(CORR_ERR_ABI, "corrx_tc_geom.struct_size=%u, expected %zu", out->struct_size,
+                     sizeof(corrx_tc_geom));
+    const TcGeom g = make_geom(n_station, split != 0, ct, kt);
+    const uint32_t size = out->struct_size;
+    *out = corrx_tc_geom{};
+    out->struct_size = size;
+    if (!g.ok) return CORR_OK;
+    out->ok = 1;
+    out->form = g.form;
+    out->elem = g.elem;
+    out->R = g.R;
+    out->nb = g.nb;
+    out->regions = g.regions;
+    out->sbo = g.sbo;
+    out->region_stride = g.region_stride;
+    out->op_stage = g.op_stage;
+    out->ld_stage = g.ld_stage;
+    out->n_op = g.n_op;
+    out->n_ld = g.n_ld;
+    out->acc_cols = g.acc_cols;
+    out->n_acc = g.n_acc;
+    out->tmem_cols = g.tmem_cols;
+    out->items = g.items;
+    out->smem = g.smem;
+    return CORR_OK;
+}
+
+namespace corrgb {
+
 void xengine_tc_default_shape(int n_station, bool split, int *ct, int *kt) {
     // 32-frame stages halve the per-stage handoffs of 16-frame ones; then the
     // widest tile that fits.

@@ -173,6 +173,25 @@ corr_status corrx_accumulate_noalloc(int32_t n_station, int32_t n_freq, int32_t 
                                      int32_t frames, void *d_acc, void *stream);
 
 /*
+ * The tensor X-engine's geometry for a tile shape, as the kernel will use it
+ * (no device work; for callers that plan shared memory or TMEM around it, and
+ * for checking the kernel's index arithmetic on a machine without a GPU).
+ * ok = 0: the shape is not feasible for n_station (everything else zero).
+ * form: 0 split stacked, 1 split wide, 2 FP16 paired, 3 FP16 wide. Operand
+ * region r starts at r*region_stride + skew(r) bytes into an operand stage,
+ * skew(r) = ((r&1) | ((r&2)<<1) | ((r&4)>>1)) * 16; row `row`, 8-frame group kq
+ * of a region lies at (row/8)*sbo + kq*128 + (row%8)*16 from its start.
+ */
+typedef struct corrx_tc_geom {
+    uint32_t struct_size;  /* sizeof(corrx_tc_geom)                                  */
+    int32_t  ok, form, elem, R, nb, regions, sbo, region_stride;
+    int32_t  op_stage, ld_stage, n_op, n_ld, acc_cols, n_acc, tmem_cols, items, smem;
+} corrx_tc_geom;
+
+corr_status corrx_tc_geometry(int32_t n_station, int32_t split, int32_t ct, int32_t kt,
+                              corrx_tc_geom *out);
+
+/*
  * On-device synthetic front end: the traffic of the reference's test transmitter
  * (corr-rs/src/bin/replay.rs), assembled into frames and a validity mask the way
  * the receive side does it (corr-rs/src/assemble.rs), written straight into

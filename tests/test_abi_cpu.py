@@ -55,6 +55,7 @@ def test_struct_layouts_match_header(pkg, tmp_path):
         "corrx_params": [f for f, _ in pkg.abi.corrx_params._fields_],
         "corrx_tiles": [f for f, _ in pkg.abi.corrx_tiles._fields_],
         "corrx_frontend": [f for f, _ in pkg.abi.corrx_frontend._fields_],
+        "corrx_tc_geom": [f for f, _ in pkg.abi.corrx_tc_geom._fields_],
         "corrw_station": [f for f, _ in pkg.abi.corrw_station._fields_],
         "corrw_params": [f for f, _ in pkg.abi.corrw_params._fields_],
         "corrw_resume": [f for f, _ in pkg.abi.corrw_resume._fields_],
