@@ -558,24 +558,39 @@ void batch_free(FxBatch *b) {
 } // namespace
 } // namespace corrgb
 
-extern "C" corr_status corrx_batch_create(void *eng, const int8_t *d_samples,
-                                          size_t station_stride, size_t frame_stride,
-                                          const uint8_t *d_mask, size_t mask_station_stride,
-                                          const int64_t *block_first, const int32_t *block_frames,
-                                          int32_t n_blocks, void *d_rows, void *h_rows,
-                                          void **out_batch) {
-    using namespace corrgb;
+namespace corrgb {
+namespace {
+
+// Capture every block into one graph; block i runs on plans[block_engine[i]]
+// (block_engine NULL: all on plans[0]).
+corr_status batch_create(const std::vector<FxPlan *> &plans, const int32_t *block_engine,
+                         const int8_t *d_samples, size_t station_stride, size_t frame_stride,
+                         const uint8_t *d_mask, size_t mask_station_stride,
+                         const int64_t *block_first, const int32_t *block_frames,
+                         int32_t n_blocks, void *d_rows, void *h_rows, void **out_batch) {
     if (out_batch == nullptr) return fail(CORR_ERR_ARG, "out_batch is NULL");
     *out_batch = nullptr;
-    FxPlan *p = static_cast<FxPlan *>(eng);
-    if (p == nullptr || d_samples == nullptr || d_rows == nullptr || block_first == nullptr ||
+    if (plans.empty()) return fail(CORR_ERR_ARG, "no engine");
+    for (FxPlan *q : plans)
+        if (q == nullptr) return fail(CORR_ERR_ARG, "an engine is NULL");
+    FxPlan *p = plans[0];
+    for (FxPlan *q : plans)
+        if (q->device != p->device || q->n_station != p->n_station || q->n_freq != p->n_freq)
+            return fail(CORR_ERR_ARG,
+                        "the engines of one batch must share device, n_station and n_freq");
+    if (d_samples == nullptr || d_rows == nullptr || block_first == nullptr ||
         block_frames == nullptr)
-        return fail(CORR_ERR_ARG, "eng, d_samples, d_rows and the block arrays must be non-NULL");
+        return fail(CORR_ERR_ARG, "d_samples, d_rows and the block arrays must be non-NULL");
     if (n_blocks < 1) return fail(CORR_ERR_ARG, "n_blocks must be >= 1");
-    for (int i = 0; i < n_blocks; ++i)
+    const int n_plans = static_cast<int>(plans.size());
+    for (int i = 0; i < n_blocks; ++i) {
         if (block_frames[i] < 1 || block_first[i] < 0)
             return failf(CORR_ERR_ARG, "block %d: first=%lld frames=%d", i,
                          (long long)block_first[i], block_frames[i]);
+        if (block_engine != nullptr && (block_engine[i] < 0 || block_engine[i] >= n_plans))
+            return failf(CORR_ERR_ARG, "block %d: engine %d of %d", i, block_engine[i], n_plans);
+    }
+    auto plan_of = [&](int i) { return plans[block_engine ? block_engine[i] : 0]; };
     corr_status st = cuda_check(cudaSetDevice(p->device), "cudaSetDevice");
     if (st != CORR_OK) return st;
     FxBatch *b = new (std::nothrow) FxBatch();
@@ -604,10 +619,16 @@ extern "C" corr_status corrx_batch_create(void *eng, const int8_t *d_samples,
         batch_free(b);
         return st;
     }
-    // Kernels configure themselves on first use; do that outside the capture.
-    st = fxplan_accumulate(p, d_samples, station_stride, frame_stride, d_mask,
-                           mask_station_stride, static_cast<int>(block_first[0]), 1, rows,
-                           b->cap);
+    // Kernels configure themselves on first use; do that outside the capture,
+    // once for every engine a block uses.
+    for (int e = 0; e < n_plans && st == CORR_OK; ++e) {
+        bool used = false;
+        for (int i = 0; i < n_blocks && !used; ++i) used = plan_of(i) == plans[e];
+        if (used)
+            st = fxplan_accumulate(plans[e], d_samples, station_stride, frame_stride, d_mask,
+                                   mask_station_stride, static_cast<int>(block_first[0]), 1,
+                                   rows, b->cap);
+    }
     if (st == CORR_OK) st = cuda_check(cudaStreamSynchronize(b->cap), "warm-up");
     if (st != CORR_OK) {
         batch_free(b);
@@ -623,7 +644,8 @@ extern "C" corr_status corrx_batch_create(void *eng, const int8_t *d_samples,
         if ((st = cuda_check(cudaMemsetAsync(row, 0, row_elems * sizeof(float2), b->cap),
                              "cudaMemsetAsync(row)")) != CORR_OK)
             break;
-        if ((st = fxplan_accumulate(p, d_samples + static_cast<size_t>(first) * frame_stride,
+        if ((st = fxplan_accumulate(plan_of(i),
+                                    d_samples + static_cast<size_t>(first) * frame_stride,
                                     station_stride, frame_stride, d_mask, mask_station_stride,
                                     first, block_frames[i], row, b->cap)) != CORR_OK)
             break;
@@ -660,6 +682,38 @@ extern "C" corr_status corrx_batch_create(void *eng, const int8_t *d_samples,
     }
     *out_batch = b;
     return CORR_OK;
+}
+
+} // namespace
+} // namespace corrgb
+
+extern "C" corr_status corrx_batch_create(void *eng, const int8_t *d_samples,
+                                          size_t station_stride, size_t frame_stride,
+                                          const uint8_t *d_mask, size_t mask_station_stride,
+                                          const int64_t *block_first, const int32_t *block_frames,
+                                          int32_t n_blocks, void *d_rows, void *h_rows,
+                                          void **out_batch) {
+    return corrgb::batch_create({static_cast<corrgb::FxPlan *>(eng)}, nullptr, d_samples,
+                                station_stride, frame_stride, d_mask, mask_station_stride,
+                                block_first, block_frames, n_blocks, d_rows, h_rows, out_batch);
+}
+
+extern "C" corr_status corrx_batch_create_mixed(void *const *engines, int32_t n_engines,
+                                                const int32_t *block_engine,
+                                                const int8_t *d_samples, size_t station_stride,
+                                                size_t frame_stride, const uint8_t *d_mask,
+                                                size_t mask_station_stride,
+                                                const int64_t *block_first,
+                                                const int32_t *block_frames, int32_t n_blocks,
+                                                void *d_rows, void *h_rows, void **out_batch) {
+    using namespace corrgb;
+    if (engines == nullptr || n_engines < 1 || block_engine == nullptr)
+        return fail(CORR_ERR_ARG, "engines, n_engines >= 1 and block_engine are required");
+    std::vector<FxPlan *> plans;
+    for (int i = 0; i < n_engines; ++i) plans.push_back(static_cast<FxPlan *>(engines[i]));
+    return batch_create(plans, block_engine, d_samples, station_stride, frame_stride, d_mask,
+                        mask_station_stride, block_first, block_frames, n_blocks, d_rows, h_rows,
+                        out_batch);
 }
 
 extern "C" corr_status corrx_batch_launch(void *batch, void *stream) {

@@ -147,6 +147,18 @@ corr_status corrx_batch_create(void *eng, const int8_t *d_samples, size_t statio
                                size_t mask_station_stride, const int64_t *block_first,
                                const int32_t *block_frames, int32_t n_blocks, void *d_rows,
                                void *h_rows, void **out_batch);
+/* corrx_batch_create with a choice of engine per block: block i runs on
+   engines[block_engine[i]] (host arrays read at creation). The engines must share
+   device, n_station and n_freq; each keeps its own spectra buffer and tiles --
+   e.g. the FP16 tensor form for blocks long enough to meet a precision target
+   and the split form for the short ones. */
+corr_status corrx_batch_create_mixed(void *const *engines, int32_t n_engines,
+                                     const int32_t *block_engine, const int8_t *d_samples,
+                                     size_t station_stride, size_t frame_stride,
+                                     const uint8_t *d_mask, size_t mask_station_stride,
+                                     const int64_t *block_first, const int32_t *block_frames,
+                                     int32_t n_blocks, void *d_rows, void *h_rows,
+                                     void **out_batch);
 corr_status corrx_batch_launch(void *batch, void *stream);
 corr_status corrx_batch_block_ms(void *batch, float *out_ms, int32_t n);
 corr_status corrx_batch_destroy(void *batch);

@@ -61,3 +61,70 @@ def test_batch_graph_rows_match_oracle(pkg, cuda, oracle, xmode):
     finally:
         lib.corrx_batch_destroy(h)
         eng.close()
+
+
+def test_mixed_engine_batch_matches_each_engine_alone(pkg, cuda, oracle):
+    """corrx_batch_create_mixed: long blocks on the FP16 form, short ones on the
+    split form; every row equals the same block run alone on its engine."""
+    torch = cuda
+    lib = pkg.abi.load()
+    n, nf, pool = 5, 1024, 400
+    rng = np.random.default_rng(9)
+    x = rng.integers(-40, 41, size=(n, pool, 2 * nf)).astype(np.int8)
+    present = rng.random((n, pool)) > 0.02
+    mask = np.packbits(present.astype(np.uint8), axis=1, bitorder="little")
+    blocks = [(0, 17), (5, 300), (120, 33), (10, 390), (64, 64)]
+    which = [1, 0, 1, 0, 1]                       # 0: FP16, 1: split
+    first = (C.c_int64 * len(blocks))(*[b[0] for b in blocks])
+    frames = (C.c_int32 * len(blocks))(*[b[1] for b in blocks])
+    sel = (C.c_int32 * len(blocks))(*which)
+    engs = [pkg.FxEngine(n, nf, max_frames=64, xmode=1), pkg.FxEngine(n, nf, max_frames=64, xmode=2)]
+    handles = (C.c_void_p * 2)(engs[0].h.value, engs[1].h.value)
+    xs = torch.from_numpy(x).cuda()
+    ms = torch.from_numpy(mask).cuda()
+    nb = n * (n + 1) // 2
+    rows = torch.zeros((len(blocks), nb, nf), dtype=torch.complex64, device="cuda")
+    h = C.c_void_p()
+    st = lib.corrx_batch_create_mixed(handles, 2, sel, C.c_void_p(xs.data_ptr()), xs.stride(0),
+                                      xs.stride(1), C.c_void_p(ms.data_ptr()), ms.stride(0),
+                                      first, frames, len(blocks), C.c_void_p(rows.data_ptr()),
+                                      None, C.byref(h))
+    assert st == 0, lib.corr_last_error()
+    stream = torch.cuda.current_stream()
+    try:
+        assert lib.corrx_batch_launch(h, C.c_void_p(stream.cuda_stream)) == 0
+        torch.cuda.synchronize()
+        for e in engs:
+            e.check()
+        got = rows.cpu().numpy()
+        lat = (C.c_float * len(blocks))()
+        assert lib.corrx_batch_block_ms(h, lat, len(blocks)) == 0
+        for i, (f0, nfr) in enumerate(blocks):
+            acc = engs[which[i]].new_acc()
+            engs[which[i]].accumulate(xs, nfr, acc, mask=ms, mask_bit0=f0, frame0=f0)
+            engs[which[i]].scale(acc, nfr)
+            torch.cuda.synchronize()
+            assert np.array_equal(got[i], acc.cpu().numpy()), i
+            ref = oracle.correlate(x[:, f0:f0 + nfr], present[:, f0:f0 + nfr]) / nfr
+            bar = 1e-5 if which[i] else 1.5e-3 / np.sqrt(nfr)
+            assert oracle.rel_rms(got[i], ref) < bar, i
+        # engines of different geometry, or a block naming no engine, are refused
+        other = pkg.FxEngine(n + 1, nf, max_frames=64, xmode=2)
+        try:
+            h2 = C.c_void_p()
+            bad = (C.c_void_p * 2)(engs[0].h.value, other.h.value)
+            assert lib.corrx_batch_create_mixed(
+                bad, 2, sel, C.c_void_p(xs.data_ptr()), xs.stride(0), xs.stride(1),
+                C.c_void_p(ms.data_ptr()), ms.stride(0), first, frames, len(blocks),
+                C.c_void_p(rows.data_ptr()), None, C.byref(h2)) == pkg.abi.CORR_ERR_ARG
+            sel_bad = (C.c_int32 * len(blocks))(0, 1, 2, 0, 1)
+            assert lib.corrx_batch_create_mixed(
+                handles, 2, sel_bad, C.c_void_p(xs.data_ptr()), xs.stride(0), xs.stride(1),
+                C.c_void_p(ms.data_ptr()), ms.stride(0), first, frames, len(blocks),
+                C.c_void_p(rows.data_ptr()), None, C.byref(h2)) == pkg.abi.CORR_ERR_ARG
+        finally:
+            other.close()
+    finally:
+        lib.corrx_batch_destroy(h)
+        for e in engs:
+            e.close()
