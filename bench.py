@@ -171,7 +171,7 @@ def run_reference(args) -> None:
     procs = os.cpu_count() or 1
     vals = []
     for _ in range(args.warmup):
-        time_cpu_oracle(w, 3.0, procs)
+        time_cpu_oracle(w, min(3.0, args.cpu_seconds), procs)
     for _ in range(args.steps):
         vals.append(time_cpu_oracle(w, args.cpu_seconds, procs))
     v = statistics.median([x["value"] for x in vals])
