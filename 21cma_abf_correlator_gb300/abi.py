@@ -276,6 +276,10 @@ SIGNATURES = {
     "corrx_frontend_fill": (C.c_int, [C.POINTER(corrx_frontend), C.c_int32, C.c_int32,
                                       C.c_int32, C.c_int64, C.c_int32, C.c_void_p, C.c_size_t, C.c_size_t,
                                       C.c_void_p, C.c_size_t, C.c_void_p]),
+    "corrx_accumulate_packets": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t,
+                                           C.c_void_p, C.c_size_t, C.c_int32, C.c_void_p,
+                                           C.c_size_t, C.c_int32, C.c_int32, C.c_void_p,
+                                           C.c_void_p]),
     "corrx_tc_geometry": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                     C.POINTER(corrx_tc_geom)]),
     "corrw_open": (C.c_int, [C.POINTER(corrw_params), C.POINTER(C.c_void_p),

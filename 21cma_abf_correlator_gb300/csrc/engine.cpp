@@ -134,7 +134,8 @@ void fxplan_destroy(FxPlan *p) {
 corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_stride,
                               size_t frame_stride, const uint8_t *mask,
                               size_t mask_station_stride, int mask_bit0, int frames,
-                              float2 *acc, cudaStream_t stream) {
+                              float2 *acc, cudaStream_t stream, const uint32_t *pmask,
+                              size_t pmask_station_stride, int pmask_frame0) {
     if (frames < 0) return fail(CORR_ERR_ARG, "frames must be >= 0");
     const size_t frame_bytes = 2u * static_cast<size_t>(p->n_freq);
     if (frame_stride < frame_bytes)
@@ -152,6 +153,9 @@ corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_s
         fa.mask = mask;
         fa.mask_station_stride = mask_station_stride;
         fa.mask_bit0 = mask_bit0 + f0;
+        fa.pmask = pmask;
+        fa.pmask_station_stride = pmask_station_stride;
+        fa.pmask_frame0 = pmask_frame0 + f0;
         fa.n_station = p->n_station;
         fa.frames = ft;
         fa.y = p->d_y;
@@ -246,6 +250,29 @@ extern "C" corr_status corrx_accumulate(void *eng, const int8_t *d_samples,
     return fxplan_accumulate(p, d_samples, station_stride, frame_stride, d_mask,
                              mask_station_stride, mask_bit0, frames,
                              static_cast<float2 *>(d_acc), static_cast<cudaStream_t>(stream));
+}
+
+extern "C" corr_status corrx_accumulate_packets(void *eng, const int8_t *d_samples,
+                                                size_t station_stride, size_t frame_stride,
+                                                const uint8_t *d_mask, size_t mask_station_stride,
+                                                int32_t mask_bit0, const uint32_t *d_pmask,
+                                                size_t pmask_station_stride,
+                                                int32_t pmask_frame0, int32_t frames,
+                                                void *d_acc, void *stream) {
+    FxPlan *p = static_cast<FxPlan *>(eng);
+    if (p == nullptr) return fail(CORR_ERR_ARG, "eng is NULL");
+    if (d_samples == nullptr || d_acc == nullptr || d_pmask == nullptr)
+        return fail(CORR_ERR_ARG, "d_samples, d_pmask and d_acc must not be NULL");
+    if (mask_bit0 < 0 || pmask_frame0 < 0)
+        return fail(CORR_ERR_ARG, "mask_bit0 and pmask_frame0 must be >= 0");
+    if (2 * p->n_freq > 32 * 1024)
+        return fail(CORR_ERR_ARG, "packet masks hold 32 packets of 1024 samples per frame");
+    corr_status st = cuda_check(cudaSetDevice(p->device), "cudaSetDevice");
+    if (st != CORR_OK) return st;
+    return fxplan_accumulate(p, d_samples, station_stride, frame_stride, d_mask,
+                             mask_station_stride, mask_bit0, frames,
+                             static_cast<float2 *>(d_acc), static_cast<cudaStream_t>(stream),
+                             d_pmask, pmask_station_stride, pmask_frame0);
 }
 
 extern "C" corr_status corrx_scale(void *eng, void *d_acc, uint64_t frames, void *stream) {

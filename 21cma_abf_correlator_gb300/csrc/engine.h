@@ -95,6 +95,11 @@ struct FengineArgs {
     const uint8_t *mask;        // nullable; bit (mask_bit0+f) of mask + s*mask_station_stride
     size_t mask_station_stride;
     int mask_bit0;
+    // nullable; word pmask[s*pmask_station_stride + pmask_frame0 + f]: bit p set = the
+    // p-th 1024-sample packet of frame f of station s arrived (the others are zeros)
+    const uint32_t *pmask;
+    size_t pmask_station_stride;
+    int pmask_frame0;
     int n_station;
     int frames;
     float2 *y;                  // spectra (y_index)
@@ -174,7 +179,9 @@ corr_status fxplan_autotune(FxPlan *p, cudaStream_t stream, corrx_tiles *out);
 corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_stride,
                               size_t frame_stride, const uint8_t *mask,
                               size_t mask_station_stride, int mask_bit0, int frames,
-                              float2 *acc, cudaStream_t stream);
+                              float2 *acc, cudaStream_t stream,
+                              const uint32_t *pmask = nullptr, size_t pmask_station_stride = 0,
+                              int pmask_frame0 = 0);
 
 /// Read and clear the device watchdog flag (synchronises the device).
 corr_status fxplan_check(FxPlan *p);

@@ -388,11 +388,29 @@ struct TwPtrs {
     const float2 *pass_lo, *pass_hi, *post_lo, *post_hi;
 };
 
+// Packets of 1024 samples (512 int8 pairs) kept for frame f of station s: all
+// of them without a packet mask, else the frame's word cut to its M/512 packets.
+template <int M>
+__host__ __device__ constexpr uint32_t all_packets() {
+    return (M >> 9) >= 32 ? 0xffffffffu : (1u << (M >> 9)) - 1u;
+}
+
+template <int M>
+__device__ __forceinline__ uint32_t packets_kept(const FengineArgs &a, int f, int s) {
+    if (a.pmask == nullptr) return all_packets<M>();
+    return a.pmask[static_cast<size_t>(s) * a.pmask_station_stride + a.pmask_frame0 + f] &
+           all_packets<M>();
+}
+
+template <int M>
 __device__ __forceinline__ bool frame_present(const FengineArgs &a, int f, int s) {
-    if (a.mask == nullptr) return true;
-    const int bit = a.mask_bit0 + f;
-    const uint8_t byte = a.mask[static_cast<size_t>(s) * a.mask_station_stride + (bit >> 3)];
-    return (byte >> (bit & 7)) & 1u;
+    if (a.mask != nullptr) {
+        const int bit = a.mask_bit0 + f;
+        const uint8_t byte = a.mask[static_cast<size_t>(s) * a.mask_station_stride + (bit >> 3)];
+        if (!((byte >> (bit & 7)) & 1u)) return false;
+    }
+    // a frame whose packets were all lost is all zeros: the same as a missing one
+    return packets_kept<M>(a, f, s) != 0u;
 }
 
 template <int LOGM, int PLAN, int FMT, bool CONTIG>
@@ -448,7 +466,7 @@ __global__ void __launch_bounds__(FeCfg<LOGM, PLAN>::T, FeCfg<LOGM, PLAN>::MIN_B
     };
     auto present = [&](int item) {
         const int f = item / a.n_station;
-        return frame_present(a, f, item - f * a.n_station);
+        return frame_present<M>(a, f, item - f * a.n_station);
     };
 
     int item = blockIdx.x;
@@ -489,6 +507,20 @@ __global__ void __launch_bounds__(FeCfg<LOGM, PLAN>::T, FeCfg<LOGM, PLAN>::MIN_B
                                kErrFengineCopyTimeout))
             *abort_flag = 1;
         parity_bits ^= 1u << buf;
+
+        if (a.pmask != nullptr) {
+            // Lost packets count as zeros: clear them in the landed copy before
+            // the first pass reads it. The word is the same for every thread,
+            // so the branch and its barrier are taken by the whole CTA.
+            const int f = item / a.n_station;
+            const uint32_t kept = packets_kept<M>(a, f, item - f * a.n_station);
+            if (kept != all_packets<M>()) {
+                uint4 *x16 = reinterpret_cast<uint4 *>(buf ? sx1 : sx0);
+                for (int i = tid; i < M / 8; i += T)     // 64 uint4 per packet
+                    if (!((kept >> (i >> 6)) & 1u)) x16[i] = make_uint4(0u, 0u, 0u, 0u);
+                __syncthreads();
+            }
+        }
 
         fft_pass<M, T, C::P, C::R0, 1, C::PADSHIFT, true>(sd, buf ? sx1 : sx0, plo, phi, tid);
         // the pass ends with a barrier: every thread sees the same flag

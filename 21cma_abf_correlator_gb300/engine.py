@@ -58,18 +58,30 @@ class FxEngine:
         return torch.zeros((self.n_baseline, self.n_freq), dtype=torch.complex64, device="cuda")
 
     def accumulate(self, samples, frames: int, acc, mask=None, mask_bit0: int = 0,
-                   stream=None, frame0: int = 0) -> None:
+                   stream=None, frame0: int = 0, packets=None, packets_frame0: int = 0) -> None:
         """acc += correlation of frames [frame0, frame0+frames) of `samples`.
 
         samples: int8 CUDA tensor [n_station, n_frames, 2*n_freq] (last dim contiguous,
         strides multiples of 16 bytes); mask: optional uint8 CUDA tensor
-        [n_station, mask_bytes] with bit (mask_bit0 + f) LSB-first per frame f.
+        [n_station, mask_bytes] with bit (mask_bit0 + f) LSB-first per frame f;
+        packets: optional int32/uint32 CUDA tensor [n_station, n_words], word
+        (packets_frame0 + f) of a station holding one bit per 1024-sample packet
+        of frame f (bit 0 first); a clear bit zero-fills that packet
+        (corrx_accumulate_packets).
         """
         assert samples.dtype.itemsize == 1 and samples.stride(2) == 1
         assert samples.shape[2] == 2 * self.n_freq and samples.shape[0] == self.n_station
         base = samples.data_ptr() + frame0 * samples.stride(1)
         mptr = 0 if mask is None else mask.data_ptr()
         mstride = 0 if mask is None else mask.stride(0)
+        if packets is not None:
+            assert packets.dtype.itemsize == 4 and packets.stride(1) == 1
+            abi.check(self.lib.corrx_accumulate_packets(
+                self.h, C.c_void_p(base), samples.stride(0), samples.stride(1),
+                C.c_void_p(mptr), mstride, mask_bit0, C.c_void_p(packets.data_ptr()),
+                packets.stride(0), packets_frame0, frames, C.c_void_p(acc.data_ptr()),
+                C.c_void_p(_stream_handle(stream))), "corrx_accumulate_packets")
+            return
         abi.check(self.lib.corrx_accumulate(
             self.h, C.c_void_p(base), samples.stride(0), samples.stride(1), C.c_void_p(mptr),
             mstride, mask_bit0, frames, C.c_void_p(acc.data_ptr()),

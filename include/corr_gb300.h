@@ -64,6 +64,22 @@ corr_status corrx_accumulate(void *eng, const int8_t *d_samples, size_t station_
                              size_t mask_station_stride, int32_t mask_bit0, int32_t frames,
                              void *d_acc, void *stream);
 
+/*
+ * corrx_accumulate with packet-granular loss: the samples of frame f of station s
+ * are taken in 1024-sample packets, and packet p counts as all zeros unless bit p
+ * of the 32-bit word d_pmask[s*pmask_station_stride + pmask_frame0 + f] is set
+ * (bit 0 = the frame's first 1024 samples). A frame with no packet left is
+ * skipped like a frame whose d_mask bit is clear (d_mask may be NULL). No
+ * counterpart in the reference, whose receive side zero-fills whole frames; its
+ * ABI path keeps that rule. 2*n_freq <= 32768 (at most 32 packets per frame).
+ */
+corr_status corrx_accumulate_packets(void *eng, const int8_t *d_samples, size_t station_stride,
+                                     size_t frame_stride, const uint8_t *d_mask,
+                                     size_t mask_station_stride, int32_t mask_bit0,
+                                     const uint32_t *d_pmask, size_t pmask_station_stride,
+                                     int32_t pmask_frame0, int32_t frames, void *d_acc,
+                                     void *stream);
+
 /* d_acc *= 1.0f/(float)frames over n_baseline*n_freq complex values. */
 corr_status corrx_scale(void *eng, void *d_acc, uint64_t frames, void *stream);
 

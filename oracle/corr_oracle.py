@@ -15,6 +15,10 @@ extended with the parts the golden generator leaves to the C driver:
                                                            corr-cuda/src/kernels.cu:159-174
   * rows divide by the caller's frame count, not the valid count
                                                            corr-cuda/include/corr_cuda.h:414-428
+and with one extension the reference does not have: a packet-granular loss mask
+(one bit per 1024-sample packet, zero_lost_packets). The reference zero-fills a
+frame whole when any of its packets is lost (corr-rs/src/assemble.rs:39-45); a
+frame whose packets are all kept or all lost gives the same result either way.
 Parity is pinned: tests/golden/ holds fixtures produced by running the
 reference's gen_golden.py itself (tests/golden/make_golden.py), and
 tests/test_oracle_golden.py checks this module against them.
@@ -59,6 +63,22 @@ def correlate(samples: np.ndarray, present: np.ndarray | None = None,
         y = np.fft.rfft(x, axis=-1)[..., :nf]             # [n, f, nf]
         acc += np.einsum("jfc,kfc->jkc", y, np.conj(y))
     return acc[iu, ju]                                    # row-major j <= k
+
+
+PACKET_SAMPLES = 1024
+
+
+def zero_lost_packets(samples: np.ndarray, kept: np.ndarray) -> np.ndarray:
+    """Copy of samples with every lost 1024-sample packet set to zero.
+
+    samples: int8 [n_station, frames, 2*n_freq]; kept: integer [n_station, frames],
+    bit p set = packet p (samples p*1024 .. p*1024+1023 of the frame) arrived.
+    """
+    n, F, L = samples.shape
+    P = L // PACKET_SAMPLES
+    bits = (kept.astype(np.uint64)[..., None] >> np.arange(P, dtype=np.uint64)) & 1
+    x = samples.reshape(n, F, P, PACKET_SAMPLES) * bits.astype(np.int8)[..., None]
+    return x.reshape(n, F, L)
 
 
 def correlate_rows(samples: np.ndarray, n_cum: int, present: np.ndarray | None = None

@@ -196,3 +196,5 @@ def test_null_context_calls(lib):
     assert lib.corr_rows_pending(None, C.byref(out)) == 1
     assert lib.corr_n_devices(None) == -1
     assert lib.corrx_accumulate(None, None, 0, 0, None, 0, 0, 0, None, None) == 1
+    assert lib.corrx_accumulate_packets(None, None, 0, 0, None, 0, 0, None, 0, 0, 0, None,
+                                        None) == 1

@@ -123,3 +123,22 @@ def test_planted_mistakes_are_caught(oracle, mistake):
         rows.append(v if mistake == "no_scale" else v / n_cum)
     wrong = np.stack(rows).astype(np.complex64)
     assert oracle.rel_rms(wrong, fx["expect"]) > 1e-3
+
+
+def test_packet_zero_fill(oracle):
+    """zero_lost_packets clears exactly the 1024-sample packets whose bit is clear;
+    all-or-nothing words reproduce the frame-granular mask."""
+    rng = np.random.default_rng(5)
+    x = rng.integers(-9, 10, size=(3, 5, 4096)).astype(np.int8)
+    kept = rng.integers(0, 16, size=(3, 5)).astype(np.uint32) | np.uint32(0xFFFFFFF0)
+    z = oracle.zero_lost_packets(x, kept)
+    for s in range(3):
+        for f in range(5):
+            for p in range(4):
+                seg, src = z[s, f, p * 1024:(p + 1) * 1024], x[s, f, p * 1024:(p + 1) * 1024]
+                assert np.array_equal(seg, src if (kept[s, f] >> p) & 1 else 0 * src)
+    present = rng.random((3, 5)) > 0.3
+    whole = np.where(present, 0xF, 0).astype(np.uint32)
+    a = oracle.correlate(oracle.zero_lost_packets(x, whole))
+    b = oracle.correlate(x, present)
+    assert np.allclose(a, b, rtol=0, atol=1e-6 * np.abs(b).max())
