@@ -285,6 +285,8 @@ __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *_
 // Bin formats: FP32 pairs; FP16 pairs scaled by `scale` (a power of two, so the
 // scaling is exact), the FP16 tensor X-engine's operands; or the split form's
 // operands, the FP16 pair h = fp16(v*scale) followed by l = fp16(v*scale - h).
+// put() takes v already multiplied by `scale`: the real-FFT split folds it
+// into its factor 1/2 (half = scale/2), which is exact for the same reason.
 // CONTIG: ytile = n_freq, one contiguous row, bin k at base[k].
 template <int FMT, bool CONTIG>
 struct YRow {
@@ -295,14 +297,15 @@ struct YRow {
     uint32_t tile_stride;  // y_frames*n_station*ytile
     int shift;             // log2(ytile)
     float scale;
+    float half;            // scale / 2
     __device__ __forceinline__ void put(int k, float2 v) const {
         T *dst = CONTIG ? base + k
                         : base + (static_cast<uint32_t>(k >> shift) * tile_stride +
                                   static_cast<uint32_t>(k & ((1 << shift) - 1)));
         if constexpr (FMT == kSpectraF16) {
-            *dst = __floats2half2_rn(v.x * scale, v.y * scale);
+            *dst = __floats2half2_rn(v.x, v.y);
         } else if constexpr (FMT == kSpectraF16Split) {
-            const float x = v.x * scale, y = v.y * scale;
+            const float x = v.x, y = v.y;
             const __half2 h = __floats2half2_rn(x, y);
             const float2 hf = __half22float2(h);
             const __half2 l = __floats2half2_rn(x - hf.x, y - hf.y);
@@ -317,12 +320,14 @@ struct YRow {
 // X[k] = Fe + w_k Fo and X[M-k] = conj(Fe - w_k Fo), with Z = FFT of the packed
 // pairs, Fe = (Z[k] + conj(Z[M-k]))/2, Fo = -i (Z[k] - conj(Z[M-k]))/2 and
 // w_k = exp(-2*pi*i*k/L) passed in. `both` = false skips X[M-k] (k = 0: Nyquist).
+// Both outputs come out multiplied by the row's scale (folded into the 1/2).
 template <class Row>
 __device__ __forceinline__ void split_store(float2 zk, float2 zmk, float2 w, int k, int M,
                                             bool both, const Row &yrow) {
     const float2 zm = make_float2(zmk.x, -zmk.y);
-    const float2 fe = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y + zm.y));
-    const float2 fo = make_float2(0.5f * (zk.y - zm.y), -0.5f * (zk.x - zm.x));
+    const float h = yrow.half;
+    const float2 fe = make_float2(h * (zk.x + zm.x), h * (zk.y + zm.y));
+    const float2 fo = make_float2(h * (zk.y - zm.y), -h * (zk.x - zm.x));
     const float2 wf = cmul(w, fo);
     yrow.put(k, cadd(fe, wf));
     if (both) yrow.put(M - k, make_float2(fe.x - wf.x, wf.y - fe.y));
@@ -381,7 +386,7 @@ __device__ __forceinline__ void last_pass_store(const float2 *__restrict__ sd,
                         yrow);
         }
     }
-    if (t0) yrow.put(M / 2, make_float2(a[H].x, -a[H].y));
+    if (t0) yrow.put(M / 2, make_float2(a[H].x * yrow.scale, -a[H].y * yrow.scale));
 }
 
 struct TwPtrs {
@@ -458,6 +463,7 @@ __global__ void __launch_bounds__(FeCfg<LOGM, PLAN>::T, FeCfg<LOGM, PLAN>::MIN_B
     const int n_items = a.frames * a.n_station;
     const uint32_t frame_bytes = 2u * M;
     const int ytile_shift = __ffs(a.ytile) - 1;
+    const float out_scale = (FMT == kSpectraF32) ? 1.0f : a.y_scale;   // FP32 bins unscaled
     auto src_of = [&](int item) {
         const int f = item / a.n_station;
         const int s = item - f * a.n_station;
@@ -491,7 +497,8 @@ __global__ void __launch_bounds__(FeCfg<LOGM, PLAN>::T, FeCfg<LOGM, PLAN>::MIN_B
         using Row = YRow<FMT, CONTIG>;
         const Row yrow{
             reinterpret_cast<typename Row::T *>(a.y) + static_cast<size_t>(item) * a.ytile,
-            static_cast<uint32_t>(a.y_frames) * a.n_station * a.ytile, ytile_shift, a.y_scale};
+            static_cast<uint32_t>(a.y_frames) * a.n_station * a.ytile, ytile_shift, out_scale,
+            0.5f * out_scale};
 
         if (!present(item)) {
             // Missing frame: its samples count as zeros, so does its spectrum.
