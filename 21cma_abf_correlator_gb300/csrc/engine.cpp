@@ -265,6 +265,8 @@ extern "C" corr_status corrx_accumulate_packets(void *eng, const int8_t *d_sampl
         return fail(CORR_ERR_ARG, "d_samples, d_pmask and d_acc must not be NULL");
     if (mask_bit0 < 0 || pmask_frame0 < 0)
         return fail(CORR_ERR_ARG, "mask_bit0 and pmask_frame0 must be >= 0");
+    if (reinterpret_cast<uintptr_t>(d_pmask) % alignof(uint32_t) != 0)
+        return fail(CORR_ERR_ARG, "d_pmask must be 4-byte aligned");
     if (2 * p->n_freq > 32 * 1024)
         return fail(CORR_ERR_ARG, "packet masks hold 32 packets of 1024 samples per frame");
     corr_status st = cuda_check(cudaSetDevice(p->device), "cudaSetDevice");

@@ -107,3 +107,25 @@ def test_every_packet_lost_is_zero(pkg, cuda):
     x, _ = inputs(n, frames, nf, seed=41)
     got = run(pkg, cuda, x, frames, kept=np.zeros((n, frames), dtype=np.uint32))
     assert not np.any(got)
+
+
+def test_bad_arguments(pkg, cuda):
+    import ctypes as C
+    n, nf, frames = 2, 1024, 4
+    eng = pkg.FxEngine(n, nf, max_frames=4)
+    acc = eng.new_acc()
+    xs = cuda.zeros((n, frames, 2 * nf), dtype=cuda.int8, device="cuda")
+    words = cuda.zeros((n, frames + 1), dtype=cuda.int32, device="cuda")
+    lib = eng.lib
+
+    def call(pm, f0=0):
+        return lib.corrx_accumulate_packets(eng.h, C.c_void_p(xs.data_ptr()), xs.stride(0),
+                                            xs.stride(1), None, 0, 0, C.c_void_p(pm), n + 1, f0,
+                                            frames, C.c_void_p(acc.data_ptr()), None)
+    assert call(words.data_ptr() + 2) == pkg.abi.CORR_ERR_ARG          # misaligned words
+    assert call(0) == pkg.abi.CORR_ERR_ARG                             # no words
+    assert call(words.data_ptr(), f0=-1) == pkg.abi.CORR_ERR_ARG       # negative word offset
+    assert call(words.data_ptr()) == pkg.abi.CORR_OK
+    cuda.cuda.synchronize()
+    eng.check()
+    eng.close()
