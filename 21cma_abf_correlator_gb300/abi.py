@@ -267,6 +267,12 @@ SIGNATURES = {
                                            C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                            C.c_int32, C.c_void_p, C.c_void_p,
                                            C.POINTER(C.c_void_p)]),
+    "corrx_batch_create_packets": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32,
+                                             C.POINTER(C.c_int32), C.c_void_p, C.c_size_t,
+                                             C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p,
+                                             C.c_size_t, C.POINTER(C.c_int64),
+                                             C.POINTER(C.c_int32), C.c_int32, C.c_void_p,
+                                             C.c_void_p, C.POINTER(C.c_void_p)]),
     "corrx_batch_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
     "corrx_batch_block_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int32]),
     "corrx_batch_destroy": (C.c_int, [C.c_void_p]),

@@ -592,9 +592,12 @@ namespace {
 
 // Capture every block into one graph; block i runs on plans[block_engine[i]]
 // (block_engine NULL: all on plans[0]).
+// d_pmask (nullable): packet words, frame f of station s at
+// d_pmask[s*pmask_station_stride + f], f counted like block_first.
 corr_status batch_create(const std::vector<FxPlan *> &plans, const int32_t *block_engine,
                          const int8_t *d_samples, size_t station_stride, size_t frame_stride,
                          const uint8_t *d_mask, size_t mask_station_stride,
+                         const uint32_t *d_pmask, size_t pmask_station_stride,
                          const int64_t *block_first, const int32_t *block_frames,
                          int32_t n_blocks, void *d_rows, void *h_rows, void **out_batch) {
     if (out_batch == nullptr) return fail(CORR_ERR_ARG, "out_batch is NULL");
@@ -611,6 +614,10 @@ corr_status batch_create(const std::vector<FxPlan *> &plans, const int32_t *bloc
         block_frames == nullptr)
         return fail(CORR_ERR_ARG, "d_samples, d_rows and the block arrays must be non-NULL");
     if (n_blocks < 1) return fail(CORR_ERR_ARG, "n_blocks must be >= 1");
+    if (d_pmask != nullptr && reinterpret_cast<uintptr_t>(d_pmask) % alignof(uint32_t) != 0)
+        return fail(CORR_ERR_ARG, "d_pmask must be 4-byte aligned");
+    if (d_pmask != nullptr && 2 * p->n_freq > 32 * 1024)
+        return fail(CORR_ERR_ARG, "packet masks hold 32 packets of 1024 samples per frame");
     const int n_plans = static_cast<int>(plans.size());
     for (int i = 0; i < n_blocks; ++i) {
         if (block_frames[i] < 1 || block_first[i] < 0)
@@ -656,7 +663,8 @@ corr_status batch_create(const std::vector<FxPlan *> &plans, const int32_t *bloc
         if (used)
             st = fxplan_accumulate(plans[e], d_samples, station_stride, frame_stride, d_mask,
                                    mask_station_stride, static_cast<int>(block_first[0]), 1,
-                                   rows, b->cap);
+                                   rows, b->cap, d_pmask, pmask_station_stride,
+                                   static_cast<int>(block_first[0]));
     }
     if (st == CORR_OK) st = cuda_check(cudaStreamSynchronize(b->cap), "warm-up");
     if (st != CORR_OK) {
@@ -676,7 +684,8 @@ corr_status batch_create(const std::vector<FxPlan *> &plans, const int32_t *bloc
         if ((st = fxplan_accumulate(plan_of(i),
                                     d_samples + static_cast<size_t>(first) * frame_stride,
                                     station_stride, frame_stride, d_mask, mask_station_stride,
-                                    first, block_frames[i], row, b->cap)) != CORR_OK)
+                                    first, block_frames[i], row, b->cap, d_pmask,
+                                    pmask_station_stride, first)) != CORR_OK)
             break;
         if ((st = scale_launch(row, row_elems, 1.0f / static_cast<float>(block_frames[i]),
                                b->cap)) != CORR_OK)
@@ -723,8 +732,8 @@ extern "C" corr_status corrx_batch_create(void *eng, const int8_t *d_samples,
                                           int32_t n_blocks, void *d_rows, void *h_rows,
                                           void **out_batch) {
     return corrgb::batch_create({static_cast<corrgb::FxPlan *>(eng)}, nullptr, d_samples,
-                                station_stride, frame_stride, d_mask, mask_station_stride,
-                                block_first, block_frames, n_blocks, d_rows, h_rows, out_batch);
+                                station_stride, frame_stride, d_mask, mask_station_stride, nullptr,
+                                0, block_first, block_frames, n_blocks, d_rows, h_rows, out_batch);
 }
 
 extern "C" corr_status corrx_batch_create_mixed(void *const *engines, int32_t n_engines,
@@ -741,8 +750,26 @@ extern "C" corr_status corrx_batch_create_mixed(void *const *engines, int32_t n_
     std::vector<FxPlan *> plans;
     for (int i = 0; i < n_engines; ++i) plans.push_back(static_cast<FxPlan *>(engines[i]));
     return batch_create(plans, block_engine, d_samples, station_stride, frame_stride, d_mask,
-                        mask_station_stride, block_first, block_frames, n_blocks, d_rows, h_rows,
-                        out_batch);
+                        mask_station_stride, nullptr, 0, block_first, block_frames, n_blocks,
+                        d_rows, h_rows, out_batch);
+}
+
+extern "C" corr_status corrx_batch_create_packets(
+    void *const *engines, int32_t n_engines, const int32_t *block_engine,
+    const int8_t *d_samples, size_t station_stride, size_t frame_stride, const uint8_t *d_mask,
+    size_t mask_station_stride, const uint32_t *d_pmask, size_t pmask_station_stride,
+    const int64_t *block_first, const int32_t *block_frames, int32_t n_blocks, void *d_rows,
+    void *h_rows, void **out_batch) {
+    using namespace corrgb;
+    if (engines == nullptr || n_engines < 1 || (n_engines > 1 && block_engine == nullptr))
+        return fail(CORR_ERR_ARG, "engines and n_engines >= 1 are required, and block_engine "
+                                  "with more than one engine");
+    if (d_pmask == nullptr) return fail(CORR_ERR_ARG, "d_pmask is NULL");
+    std::vector<FxPlan *> plans;
+    for (int i = 0; i < n_engines; ++i) plans.push_back(static_cast<FxPlan *>(engines[i]));
+    return batch_create(plans, block_engine, d_samples, station_stride, frame_stride, d_mask,
+                        mask_station_stride, d_pmask, pmask_station_stride, block_first,
+                        block_frames, n_blocks, d_rows, h_rows, out_batch);
 }
 
 extern "C" corr_status corrx_batch_launch(void *batch, void *stream) {

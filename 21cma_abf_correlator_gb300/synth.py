@@ -6,8 +6,11 @@ with n_i and s independent N(0,1) streams, d_i an integer delay drawn from the
 seed, and optional tones A*cos(2*pi*ch*t/L) (bin `ch` of the L = 2*n_freq FFT).
 Packet loss: each 1024-sample packet of each input is lost with probability p;
 a frame with any lost packet is declared missing in the validity mask, which is
-the reference's frame-granular rule (corr-rs/src/assemble.rs:39-45). No public
-dataset is involved; these stand in for the front-end streams.
+the reference's frame-granular rule (corr-rs/src/assemble.rs:39-45). With
+`words=True` the generators also return the packet-granular form of the same
+loss: one 32-bit word per (input, frame), bit p set when packet p arrived
+(corrx_accumulate_packets). No public dataset is involved; these stand in for
+the front-end streams.
 
 Two back ends with the same model: numpy (CPU; small cases, the oracle's
 inputs) and torch on the GPU (large cases; bench inputs are generated in HBM,
@@ -79,8 +82,9 @@ def _tone_inputs(w: Workload, tone) -> range:
     return range(n)
 
 
-def generate_numpy(w: Workload, frames: int, seed_offset: int = 0):
-    """(samples int8 [N, frames, L], mask uint8 [N, ceil(frames/8)] or None)."""
+def generate_numpy(w: Workload, frames: int, seed_offset: int = 0, words: bool = False):
+    """(samples int8 [N, frames, L], mask uint8 [N, ceil(frames/8)] or None)
+    [+ packet words uint32 [N, frames] or None with words=True]."""
     L = w.fft_len
     T = frames * L
     rng = np.random.default_rng([w.seed, seed_offset])
@@ -96,10 +100,14 @@ def generate_numpy(w: Workload, frames: int, seed_offset: int = 0):
             if i in _tone_inputs(w, tone):
                 x += tone[1] * np.cos(2.0 * np.pi * tone[0] * (t % L) / L)
         out[i] = np.clip(np.rint(x), -128, 127).astype(np.int8).reshape(frames, L)
-    mask = None
+    mask = kept = None
     if w.loss > 0:
-        mask = loss_mask_numpy(w, frames, rng)
-    return out, mask
+        per_frame = w.fft_len // PACKET_SAMPLES
+        lost = rng.random((w.n_station, frames, per_frame)) < w.loss
+        mask = pack_mask(~lost.any(axis=2))
+        kept = ((~lost).astype(np.uint64) << np.arange(per_frame, dtype=np.uint64)).sum(
+            axis=2).astype(np.uint32)
+    return (out, mask, kept) if words else (out, mask)
 
 
 def loss_mask_numpy(w: Workload, frames: int, rng) -> np.ndarray:
@@ -118,8 +126,10 @@ def unpack_mask(mask: np.ndarray, frames: int) -> np.ndarray:
     return np.unpackbits(mask, axis=1, bitorder="little")[:, :frames].astype(bool)
 
 
-def generate_torch(w: Workload, frames: int, seed_offset: int = 0, device: str = "cuda"):
-    """Same model on the GPU with torch's generator: (int8 [N, frames, L], uint8 mask or None)."""
+def generate_torch(w: Workload, frames: int, seed_offset: int = 0, device: str = "cuda",
+                   words: bool = False):
+    """Same model on the GPU with torch's generator: (int8 [N, frames, L], uint8 mask or None)
+    [+ packet words int32 [N, frames] (bit patterns of uint32) or None with words=True]."""
     import torch
     L = w.fft_len
     T = frames * L
@@ -144,10 +154,14 @@ def generate_torch(w: Workload, frames: int, seed_offset: int = 0, device: str =
         out[i] = xv.round_().clamp_(-128, 127).to(torch.int8)
         del x, xv
     del s
-    mask = None
+    mask = kept = None
     if w.loss > 0:
         per_frame = L // PACKET_SAMPLES
         lost = torch.rand((w.n_station, frames, per_frame), generator=g, device=device) < w.loss
+        if words:
+            bits = torch.arange(per_frame, device=device, dtype=torch.int64)
+            k64 = ((~lost).to(torch.int64) << bits).sum(dim=2)
+            kept = torch.where(k64 >= 2 ** 31, k64 - 2 ** 32, k64).to(torch.int32)
         present = (~lost.any(dim=2)).to(torch.uint8)
         nb = mask_bytes(frames)
         pad = nb * 8 - frames
@@ -157,7 +171,7 @@ def generate_torch(w: Workload, frames: int, seed_offset: int = 0, device: str =
         weights = (2 ** torch.arange(8, device=device, dtype=torch.int32)).view(1, 1, 8)
         mask = (present.view(w.n_station, nb, 8).to(torch.int32) * weights).sum(dim=2).to(
             torch.uint8)
-    return out, mask
+    return (out, mask, kept) if words else (out, mask)
 
 
 def block_plan(w: Workload, seed_offset: int = 0) -> list[tuple[int, int]]:

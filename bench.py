@@ -511,11 +511,14 @@ def run_batching(pkg, synth, torch, stream, forms) -> dict:
 
     forms: [(xmode, name, min_frames), ...] in order of preference; each block
     runs on the first form whose min_frames it reaches (one engine per form,
-    corrx_batch_create_mixed when there are several)."""
+    corrx_batch_create_mixed when there are several). The packet loss is applied
+    twice: at frame granularity (a frame with a lost packet is zeroed whole, the
+    reference's receive rule; the main figures) and at packet granularity (only
+    the lost 1024-sample packets are zeroed, corrx_batch_create_packets)."""
     import ctypes as C
     abi = pkg.abi
     w = synth.WORKLOADS["batching-24in-nf16384"]
-    pool, mask = synth.generate_torch(w, w.frames)            # 8192-frame ring
+    pool, mask, words = synth.generate_torch(w, w.frames, words=True)   # 8192-frame ring
     plan = synth.block_plan(w)
     nblk = len(plan)
     engs = []
@@ -531,38 +534,60 @@ def run_batching(pkg, synth, torch, stream, forms) -> dict:
     sel = (C.c_int32 * nblk)(*which)
     handles = (C.c_void_p * len(engs))(*[e_.h.value for e_ in engs])
     lib = engs[0].lib
-    h = C.c_void_p()
-    abi.check(lib.corrx_batch_create_mixed(
-        handles, len(engs), sel, C.c_void_p(pool.data_ptr()), pool.stride(0), pool.stride(1),
-        C.c_void_p(mask.data_ptr()), mask.stride(0), first, frames, nblk,
-        C.c_void_p(rows.data_ptr()), C.c_void_p(host.data_ptr()), C.byref(h)),
-        "corrx_batch_create_mixed")
-    try:
-        abi.check(lib.corrx_batch_launch(h, C.c_void_p(stream.cuda_stream)), "launch")
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        abi.check(lib.corrx_batch_launch(h, C.c_void_p(stream.cuda_stream)), "launch")
-        e1.record(stream)
-        torch.cuda.synchronize()
-        for e_ in engs:
-            e_.check()
-        ms = e0.elapsed_time(e1)
-        lat = (C.c_float * nblk)()
-        abi.check(lib.corrx_batch_block_ms(h, lat, nblk), "corrx_batch_block_ms")
-    finally:
-        lib.corrx_batch_destroy(h)
-        for e_ in engs:
-            e_.close()
     total_frames = sum(b[1] for b in plan)
     samples = w.n_station * total_frames * w.fft_len
-    lat = np.array(list(lat))
+
+    def timed(packets: bool) -> dict:
+        h = C.c_void_p()
+        common = (C.c_void_p(pool.data_ptr()), pool.stride(0), pool.stride(1))
+        if packets:
+            abi.check(lib.corrx_batch_create_packets(
+                handles, len(engs), sel, *common, None, 0, C.c_void_p(words.data_ptr()),
+                words.stride(0), first, frames, nblk, C.c_void_p(rows.data_ptr()),
+                C.c_void_p(host.data_ptr()), C.byref(h)), "corrx_batch_create_packets")
+        else:
+            abi.check(lib.corrx_batch_create_mixed(
+                handles, len(engs), sel, *common, C.c_void_p(mask.data_ptr()), mask.stride(0),
+                first, frames, nblk, C.c_void_p(rows.data_ptr()), C.c_void_p(host.data_ptr()),
+                C.byref(h)), "corrx_batch_create_mixed")
+        try:
+            abi.check(lib.corrx_batch_launch(h, C.c_void_p(stream.cuda_stream)), "launch")
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            abi.check(lib.corrx_batch_launch(h, C.c_void_p(stream.cuda_stream)), "launch")
+            e1.record(stream)
+            torch.cuda.synchronize()
+            for e_ in engs:
+                e_.check()
+            ms = e0.elapsed_time(e1)
+            lat = (C.c_float * nblk)()
+            abi.check(lib.corrx_batch_block_ms(h, lat, nblk), "corrx_batch_block_ms")
+        finally:
+            lib.corrx_batch_destroy(h)
+        lat = np.array(list(lat))
+        return {"value": samples / (ms * 1e-3) / 1e9, "ms_per_launch": ms,
+                "latency_ms": {"p50": float(np.percentile(lat, 50)),
+                               "p99": float(np.percentile(lat, 99)),
+                               "max": float(lat.max())}}
+
+    try:
+        by_frame = timed(False)
+        by_packet = timed(True)
+    finally:
+        for e_ in engs:
+            e_.close()
+    n_lost = int(((words.to(torch.int64) & 0xFFFFFFFF) != 0xFFFFFFFF).sum())
     return {"workload": w.name, "blocks": nblk, "frames_total": total_frames,
-            "value": samples / (ms * 1e-3) / 1e9, "unit": "GSample/s", "ms_per_launch": ms,
-            "graph_launches": 1, "latency_ms": {"p50": float(np.percentile(lat, 50)),
-                                                "p99": float(np.percentile(lat, 99)),
-                                                "max": float(lat.max())},
+            "value": by_frame["value"], "unit": "GSample/s",
+            "ms_per_launch": by_frame["ms_per_launch"], "graph_launches": 1,
+            "latency_ms": by_frame["latency_ms"],
             "latency": "block start to its row in pinned host memory, inside the graph",
+            "loss": f"{w.loss:.3%} of 1024-sample packets; frame-granular zero-fill (a frame "
+                    f"with a lost packet is zeroed whole): {n_lost} of {words.numel()} "
+                    f"pool frames",
+            "packet_granular": dict(by_packet, loss="only the lost packets zero-filled "
+                                                    "(corrx_batch_create_packets)"),
             "xengine": {f[1]: {"blocks": which.count(i), "min_frames": f[2]}
                         for i, f in enumerate(forms)}}
 
@@ -570,7 +595,7 @@ def run_batching(pkg, synth, torch, stream, forms) -> dict:
 def run_stream(pkg, synth, torch, stream) -> dict:
     """40 inputs at 250 MS/s each: one 4096-frame integration with the split engine."""
     w = synth.WORKLOADS["stream-40in-nf16384"]
-    x, mask = synth.generate_torch(w, w.frames)
+    x, mask, words = synth.generate_torch(w, w.frames, words=True)
     eng = pkg.FxEngine(w.n_station, w.n_freq, PASS_FRAMES,
                        xmode=pkg.abi.CORR_X_TC_FP16_SPLIT)
     tiles = eng.autotune(stream)
@@ -612,6 +637,23 @@ def run_stream(pkg, synth, torch, stream) -> dict:
     torch.cuda.synchronize()
     lat = sorted(marks[i].elapsed_time(ends[i]) for i in range(n_int))
     total_ms = marks[0].elapsed_time(marks[n_int])
+    # the same integration with only the lost packets zero-filled
+    wd = words.contiguous()
+
+    def step_packets():
+        acc.zero_()
+        eng.accumulate(x, w.frames, acc, stream=stream, packets=wd)
+        eng.scale(acc, w.frames, stream=stream)
+    step_packets()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(2):
+        step_packets()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    eng.check()
+    ms_pk = e0.elapsed_time(e1) / 2
+    acc_pk = accuracy_report(torch, w, x, None, {"tc_split": acc.clone()}, words=wd)
     # the F-engine alone on one pass: algorithmic HBM bytes / time
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     lib = eng.lib
@@ -649,19 +691,30 @@ def run_stream(pkg, synth, torch, stream) -> dict:
                         "frac_of_hbm": f_bytes / (t_f * 1e-3) / 1e9 / hbm, "peak_kind": kind},
             "accuracy_first_integration": {"channels": acc_rep["channels"],
                                            "baselines": acc_rep["baselines"],
-                                           "vs_fp64": acc_rep["vs_fp64"]["tc_split"]}}
+                                           "vs_fp64": acc_rep["vs_fp64"]["tc_split"]},
+            "loss": f"{w.loss:.3%} of 1024-sample packets; frame-granular zero-fill (a frame "
+                    f"with a lost packet is zeroed whole, the reference's rule)",
+            "packet_granular": {
+                "value": w.n_station * w.frames * w.fft_len / (ms_pk * 1e-3) / 1e9,
+                "ms_per_integration": ms_pk,
+                "real_time_factor": w.n_station * w.frames * w.fft_len / (ms_pk * 1e-3) / 1e9
+                / need,
+                "loss": "only the lost packets zero-filled (corrx_accumulate_packets)",
+                "accuracy_first_integration_vs_fp64": acc_pk["vs_fp64"]["tc_split"]}}
 
 
 ACCURACY_CHANNELS = [0, 1, 2, 63, 1234, 2047, 3000, 4096, 5555, 8191, 8192, 9000, 12345,
                      16000, 16382, 16383]
 
 
-def accuracy_report(torch, w, x, mask, rows: dict, channels=ACCURACY_CHANNELS) -> dict:
+def accuracy_report(torch, w, x, mask, rows: dict, channels=ACCURACY_CHANNELS,
+                    words=None) -> dict:
     """Errors of each path's rows for one integration (already divided by frames).
 
     vs_fp64: against an exact float64 DFT of every frame at `channels` (all
-    baselines; lost frames zeroed as the engines do), computed on the device
-    in float64 with matrix products of the int8 frames and the DFT columns.
+    baselines; lost frames zeroed as the engines do, and with `words` the lost
+    1024-sample packets), computed on the device in float64 with matrix
+    products of the int8 frames and the DFT columns.
     vs_plain: each tensor form against the plain FP32 path over the whole row.
     rel_rms = ||V - V_ref|| / ||V_ref||; max_per_vis = max |V - V_ref| /
     sqrt(|V_jj V_kk|) (the error relative to the two inputs' powers);
@@ -684,6 +737,11 @@ def accuracy_report(torch, w, x, mask, rows: dict, channels=ACCURACY_CHANNELS) -
                 fr = torch.arange(f0, min(f0 + step, F), device=dev)
                 bits = (mask[s_, fr // 8].to(torch.int64) >> (fr % 8)) & 1
                 blk = blk * bits.to(torch.float64)[:, None]
+            if words is not None:
+                P = L // 1024
+                wd = words[s_, f0:f0 + step].to(torch.int64)[:, None]
+                keep = (wd >> torch.arange(P, device=dev)) & 1                  # [f, P]
+                blk = (blk.view(-1, P, 1024) * keep.to(torch.float64)[:, :, None]).view(-1, L)
             prod = blk @ Wm
             Y[s_, f0:f0 + step] = torch.complex(prod[:, :C_], prod[:, C_:])
     pairs = [(j, k) for j in range(N) for k in range(j, N)]

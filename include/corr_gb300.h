@@ -175,6 +175,18 @@ corr_status corrx_batch_create_mixed(void *const *engines, int32_t n_engines,
                                      const int64_t *block_first, const int32_t *block_frames,
                                      int32_t n_blocks, void *d_rows, void *h_rows,
                                      void **out_batch);
+/* corrx_batch_create_mixed with packet-granular loss (corrx_accumulate_packets'
+   rule): frame f of station s keeps the 1024-sample packets whose bits are set
+   in d_pmask[s*pmask_station_stride + f], f counted like block_first. d_mask may
+   be NULL; block_engine may be NULL with one engine. */
+corr_status corrx_batch_create_packets(void *const *engines, int32_t n_engines,
+                                       const int32_t *block_engine, const int8_t *d_samples,
+                                       size_t station_stride, size_t frame_stride,
+                                       const uint8_t *d_mask, size_t mask_station_stride,
+                                       const uint32_t *d_pmask, size_t pmask_station_stride,
+                                       const int64_t *block_first, const int32_t *block_frames,
+                                       int32_t n_blocks, void *d_rows, void *h_rows,
+                                       void **out_batch);
 corr_status corrx_batch_launch(void *batch, void *stream);
 corr_status corrx_batch_block_ms(void *batch, float *out_ms, int32_t n);
 corr_status corrx_batch_destroy(void *batch);

@@ -129,3 +129,19 @@ def test_bad_arguments(pkg, cuda):
     cuda.cuda.synchronize()
     eng.check()
     eng.close()
+
+
+@pytest.mark.parametrize("xmode,tol", [(0, 1e-5), (2, 1e-5)])
+def test_plain_gpu_workload_with_packet_loss(pkg, cuda, oracle, xmode, tol):
+    """The 20-input n_freq 8192 workload with its 0.1 % packet loss applied per
+    packet (16 packets per frame) rather than per frame."""
+    import importlib
+    synth = importlib.import_module(pkg.__name__ + ".synth")
+    w = synth.WORKLOADS["plain-gpu-20in-nf8192"]
+    frames = 48
+    x, mask, kept = synth.generate_numpy(w, frames, words=True)
+    assert kept is not None and (kept != (1 << 16) - 1).any()
+    ref = oracle.correlate(oracle.zero_lost_packets(x, kept))
+    got = run(pkg, cuda, x, frames, xmode=xmode, kept=kept)
+    assert oracle.rel_rms(got, ref) <= tol
+    assert oracle.normalized_max_err(got, ref, w.n_station) <= 2 * tol
