@@ -354,6 +354,9 @@ corr_status fxplan_set_tiles(FxPlan *p, int ytile, int xct, int xkt, int fplan) 
     if (fplan < 0 || fplan >= fengine_plans(p->n_freq))
         return failf(CORR_ERR_ARG, "FFT plan %d: n_freq=%d has plans 0..%d", fplan, p->n_freq,
                      fengine_plans(p->n_freq) - 1);
+    if (!fengine_plan_ok(p->n_freq, fplan, spectra_format(p->xmode)))
+        return failf(CORR_ERR_ARG, "FFT plan %d does not write the spectra of X-engine mode %d",
+                     fplan, p->xmode);
     if (ytile < 2 || ytile > p->n_freq || (ytile & (ytile - 1)) != 0)
         return failf(CORR_ERR_ARG, "ytile=%d is not a power of two in [2, n_freq=%d]", ytile,
                      p->n_freq);
@@ -454,6 +457,7 @@ corr_status fxplan_autotune(FxPlan *p, cudaStream_t stream, corrx_tiles *out) {
     int best_fplan = fplan0;
     Cand best{ytile0, ct0, kt0};
     for (int fp = 0; fp < n_fplans && st == CORR_OK; ++fp) {
+        if (!fengine_plan_ok(p->n_freq, fp, spectra_format(p->xmode))) continue;
         if ((st = fxplan_set_tiles(p, p->n_freq, cands[0].ct, cands[0].kt, fp)) != CORR_OK) break;
         float f_ms = 0.f;
         if ((st = timed(run_f, &f_ms)) != CORR_OK) break;

@@ -52,6 +52,7 @@ struct TwiddleTables {
     float2 *post_hi = nullptr;
     int n_pass_hi = 0;
     int n_post_hi = 0;
+    void *tc_image = nullptr;   // tensor-core FFT tables (plan 2, n_freq 16384)
 };
 
 /// Spectra layout shared by the F- and X-engines: channel tiles of `ytile`
@@ -129,6 +130,12 @@ corr_status fengine_prepare(int n_freq, TwiddleTables *tw);
 /// How many FFT radix plans the F-engine has for n_freq (plan 0 always exists).
 int fengine_plans(int n_freq);
 void fengine_release(TwiddleTables *tw);
+/// FFT plan 2 (n_freq 16384, FP16 spectra): the tensor-core F-engine (fengine_tc.cu).
+corr_status fengine_tc_prepare(void **d_image);
+corr_status fengine_tc_launch(const FengineArgs &a, const void *image, int num_sms,
+                              cudaStream_t stream);
+/// Whether FFT plan `fplan` can write spectra of format `y_fmt` at n_freq.
+bool fengine_plan_ok(int n_freq, int fplan, int y_fmt);
 corr_status fengine_launch(int n_freq, const TwiddleTables &tw, const FengineArgs &a,
                            int num_sms, cudaStream_t stream);
 

@@ -30,6 +30,7 @@
 #include <cuda_fp16.h>
 
 #include "engine.h"
+#include "fft_common.cuh"
 #include "ptx.cuh"
 
 namespace corrgb {
@@ -39,37 +40,6 @@ namespace {
 // Small DFTs in registers, forward sign (exp(-2*pi*i*n*k/R)), natural order.
 // All constant twiddles are 32nd roots of unity.
 // ---------------------------------------------------------------------------
-
-// cos(2*pi*m/32) and sin(2*pi*m/32) for m in [0, 32), built from the first octant.
-__host__ __device__ constexpr float cos32_q(int r) {
-    return r == 0 ? 1.0f
-         : r == 1 ? 0.98078528040323044913f
-         : r == 2 ? 0.92387953251128675613f
-         : r == 3 ? 0.83146961230254523708f
-         : r == 4 ? 0.70710678118654752440f
-         : r == 5 ? 0.55557023301960222474f
-         : r == 6 ? 0.38268343236508977173f
-         : r == 7 ? 0.19509032201612826785f
-                  : 0.0f;
-}
-__host__ __device__ constexpr float cos32(int m) {
-    return (m & 31) < 8    ? cos32_q(m & 31)
-         : (m & 31) < 16 ? -cos32_q(16 - (m & 31))
-         : (m & 31) < 24 ? -cos32_q((m & 31) - 16)
-                         : cos32_q(32 - (m & 31));
-}
-__host__ __device__ constexpr float sin32(int m) { return cos32(m - 8); }
-
-// a * exp(-2*pi*i*m/32); m is a compile-time constant after unrolling.
-__device__ __forceinline__ float2 mul_w32(float2 a, int m) {
-    m &= 31;
-    if (m == 0) return a;
-    if (m == 8) return make_float2(a.y, -a.x);
-    if (m == 16) return make_float2(-a.x, -a.y);
-    if (m == 24) return make_float2(-a.y, a.x);
-    const float c = cos32(m), s = sin32(m);
-    return make_float2(fmaf(a.x, c, a.y * s), fmaf(a.y, c, -a.x * s));
-}
 
 template <int R>
 struct Dft;
@@ -280,59 +250,6 @@ __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *_
     __syncthreads();
 }
 
-// Where bin k of the current (frame, station) goes in the channel-tiled layout.
-// (Element indices fit 32 bits: the spectra buffer holds < 2^32 values.)
-// Bin formats: FP32 pairs; FP16 pairs scaled by `scale` (a power of two, so the
-// scaling is exact), the FP16 tensor X-engine's operands; or the split form's
-// operands, the FP16 pair h = fp16(v*scale) followed by l = fp16(v*scale - h).
-// put() takes v already multiplied by `scale`: the real-FFT split folds it
-// into its factor 1/2 (half = scale/2), which is exact for the same reason.
-// CONTIG: ytile = n_freq, one contiguous row, bin k at base[k].
-template <int FMT, bool CONTIG>
-struct YRow {
-    using T = typename std::conditional<
-        FMT == kSpectraF32, float2,
-        typename std::conditional<FMT == kSpectraF16, __half2, uint2>::type>::type;
-    T *base;               // y + (f*n_station + s)*ytile
-    uint32_t tile_stride;  // y_frames*n_station*ytile
-    int shift;             // log2(ytile)
-    float scale;
-    float half;            // scale / 2
-    __device__ __forceinline__ void put(int k, float2 v) const {
-        T *dst = CONTIG ? base + k
-                        : base + (static_cast<uint32_t>(k >> shift) * tile_stride +
-                                  static_cast<uint32_t>(k & ((1 << shift) - 1)));
-        if constexpr (FMT == kSpectraF16) {
-            *dst = __floats2half2_rn(v.x, v.y);
-        } else if constexpr (FMT == kSpectraF16Split) {
-            const float x = v.x, y = v.y;
-            const __half2 h = __floats2half2_rn(x, y);
-            const float2 hf = __half22float2(h);
-            const __half2 l = __floats2half2_rn(x - hf.x, y - hf.y);
-            *dst = make_uint2(*reinterpret_cast<const uint32_t *>(&h),
-                              *reinterpret_cast<const uint32_t *>(&l));
-        } else {
-            *dst = v;
-        }
-    }
-};
-
-// X[k] = Fe + w_k Fo and X[M-k] = conj(Fe - w_k Fo), with Z = FFT of the packed
-// pairs, Fe = (Z[k] + conj(Z[M-k]))/2, Fo = -i (Z[k] - conj(Z[M-k]))/2 and
-// w_k = exp(-2*pi*i*k/L) passed in. `both` = false skips X[M-k] (k = 0: Nyquist).
-// Both outputs come out multiplied by the row's scale (folded into the 1/2).
-template <class Row>
-__device__ __forceinline__ void split_store(float2 zk, float2 zmk, float2 w, int k, int M,
-                                            bool both, const Row &yrow) {
-    const float2 zm = make_float2(zmk.x, -zmk.y);
-    const float h = yrow.half;
-    const float2 fe = make_float2(h * (zk.x + zm.x), h * (zk.y + zm.y));
-    const float2 fo = make_float2(h * (zk.y - zm.y), -h * (zk.x - zm.x));
-    const float2 wf = cmul(w, fo);
-    yrow.put(k, cadd(fe, wf));
-    if (both) yrow.put(M - k, make_float2(fe.x - wf.x, wf.y - fe.y));
-}
-
 // Last pass (radix R2, NS = J) fused with the split and the global store.
 // Thread t >= 1 owns butterflies t and J - t: Z[M - (t + r*J)] = Z[(J - t) + (R-1-r)*J],
 // so its R pairs are (a[r], b[R-1-r]). Thread 0 owns the two self-paired
@@ -392,31 +309,6 @@ __device__ __forceinline__ void last_pass_store(const float2 *__restrict__ sd,
 struct TwPtrs {
     const float2 *pass_lo, *pass_hi, *post_lo, *post_hi;
 };
-
-// Packets of 1024 samples (512 int8 pairs) kept for frame f of station s: all
-// of them without a packet mask, else the frame's word cut to its M/512 packets.
-template <int M>
-__host__ __device__ constexpr uint32_t all_packets() {
-    return (M >> 9) >= 32 ? 0xffffffffu : (1u << (M >> 9)) - 1u;
-}
-
-template <int M>
-__device__ __forceinline__ uint32_t packets_kept(const FengineArgs &a, int f, int s) {
-    if (a.pmask == nullptr) return all_packets<M>();
-    return a.pmask[static_cast<size_t>(s) * a.pmask_station_stride + a.pmask_frame0 + f] &
-           all_packets<M>();
-}
-
-template <int M>
-__device__ __forceinline__ bool frame_present(const FengineArgs &a, int f, int s) {
-    if (a.mask != nullptr) {
-        const int bit = a.mask_bit0 + f;
-        const uint8_t byte = a.mask[static_cast<size_t>(s) * a.mask_station_stride + (bit >> 3)];
-        if (!((byte >> (bit & 7)) & 1u)) return false;
-    }
-    // a frame whose packets were all lost is all zeros: the same as a missing one
-    return packets_kept<M>(a, f, s) != 0u;
-}
 
 template <int LOGM, int PLAN, int FMT, bool CONTIG>
 __global__ void __launch_bounds__(FeCfg<LOGM, PLAN>::T, FeCfg<LOGM, PLAN>::MIN_BLOCKS)
@@ -597,6 +489,7 @@ corr_status launch_size(const FengineArgs &a, const TwiddleTables &tw, int num_s
                         cudaStream_t stream) {
     if constexpr (LOGM == 14) {
         if (a.fplan == 1) return launch_plan<LOGM, 1>(a, tw, num_sms, stream);
+        if (a.fplan == 2) return fengine_tc_launch(a, tw.tc_image, num_sms, stream);
     }
     if (a.fplan != 0)
         return failf(CORR_ERR_ARG, "FFT plan %d is not available at n_freq=%d", a.fplan, 1 << LOGM);
@@ -611,7 +504,12 @@ int ilog2(int v) {
 
 } // namespace
 
-int fengine_plans(int n_freq) { return n_freq == 16384 ? 2 : 1; }
+int fengine_plans(int n_freq) { return n_freq == 16384 ? 3 : 1; }
+
+bool fengine_plan_ok(int n_freq, int fplan, int y_fmt) {
+    if (fplan < 0 || fplan >= fengine_plans(n_freq)) return false;
+    return fplan != 2 || y_fmt == kSpectraF16;   // the tensor-core plan writes FP16 only
+}
 
 corr_status fengine_prepare(int n_freq, TwiddleTables *tw) {
     const int M = n_freq;
@@ -654,11 +552,16 @@ corr_status fengine_prepare(int n_freq, TwiddleTables *tw) {
     tw->pass_hi = d + 64;
     tw->post_lo = tw->pass_hi + h_phi.size();
     tw->post_hi = tw->post_lo + 64;
+    if (n_freq == 16384 && (st = fengine_tc_prepare(&tw->tc_image)) != CORR_OK) {
+        fengine_release(tw);
+        return st;
+    }
     return CORR_OK;
 }
 
 void fengine_release(TwiddleTables *tw) {
     if (tw->pass_lo != nullptr) cudaFree(tw->pass_lo);
+    if (tw->tc_image != nullptr) cudaFree(tw->tc_image);
     *tw = TwiddleTables{};
 }
 

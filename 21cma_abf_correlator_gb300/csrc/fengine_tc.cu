@@ -1,0 +1,594 @@
+// fengine_tc.cu -- the F-engine on the tensor cores: n_freq 16384, FP16 spectra.
+//
+// FFT plan 2 at n_freq 16384 for the FP16 tensor X-engine. A frame's 32768
+// int8 samples, packed as M = 16384 complex points z[n] = x[2n] + i x[2n+1],
+// are transformed by three DFT stages, each a matrix product on tcgen05
+// (kind::f16, FP32 accumulators in TMEM):
+//
+//   n = 512 a + b,  b = 16 c + d;   k = k1 + 32 k2a + 1024 k2b
+//   stage 1: DFT-32 over a  for the 512 rows b          -> k1, then * W_M^(b k1)
+//   stage 2: DFT-32 over c  for the 512 rows (k1, d)    -> k2a, then * W_512^(d k2a)
+//   stage 3: DFT-16 over d  for the 1024 rows (k1, k2a) -> k2b
+//
+// A stage's operand A (rows x the DFT's inputs, re/im interleaved along K) is
+// FP16 in shared memory in the K-major no-swizzle layout (8-row x 16-byte core
+// matrices); the DFT matrices (real 2R x 2R forms) are the B operands, each the
+// sum of an FP16 "hi" and "lo" part issued as two MMAs into one accumulator,
+// so the matrices carry about 22 bits and the data one FP16 rounding per stage.
+// The twiddles between the stages, the FP16 conversion and the real-FFT split
+// after stage 3 run on the CUDA cores, which read the accumulators with
+// tcgen05.ld. Rows are ordered so that every stage's scatter into the next
+// operand is free of shared-memory bank conflicts where it matters, and so that
+// after stage 3 the rows holding Z[k] and Z[M-k] sit in the same TMEM lane of
+// two tiles (one thread does the split of both).
+//
+// Magnitudes: |z| <= 180, stage 1 outputs <= 5760 (FP16 holds them), stage 2
+// outputs are scaled by 1/32 (folded into its twiddle table) before FP16, and
+// stage 3 stays in FP32. The spectrum goes out as FP16 pairs scaled by
+// y_scale (x32 to undo the 1/32), exactly as the CUDA-core F-engine writes them.
+//
+// One CTA per SM (168 KB of shared memory, 256 TMEM columns), persistent over
+// (frame, station) items like fengine.cu: the next item's int8 frame arrives by
+// a TMA bulk copy while the current one is transformed; missing frames and
+// lost packets are handled the same way. Within an item the stages run in
+// order: all warps convert, one thread issues the MMAs, all warps wait for them
+// (clock-bounded mbarrier waits) and run the epilogue.
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include <cuda_fp16.h>
+
+#include "engine.h"
+#include "fft_common.cuh"
+#include "ptx.cuh"
+
+namespace corrgb {
+namespace {
+
+constexpr int kM = 16384;
+constexpr int kThreads = 512;
+constexpr int kLBO = 128;                 // bytes between K-adjacent core matrices
+constexpr int kSboA12 = 1024;             // stages 1, 2: 512 rows x 64 FP16 per row
+constexpr int kSboA3 = 512;               // stage 3: 1024 rows x 32 FP16 per row
+constexpr int kSboB1 = 1024;              // DFT-32 (64 x 64)
+constexpr int kSboB3 = 512;               // DFT-16 (32 x 32)
+constexpr int kB1Bytes = 64 * 64 * 2;
+constexpr int kB3Bytes = 32 * 32 * 2;
+constexpr int kTw1 = 512;                 // W_M^b, b < 512
+constexpr int kTw2 = 512;                 // W_512^(d k2a) / 32, [k2a][d]
+constexpr int kTw3 = 520;                 // exp(-2 pi i k / L), k <= 512
+constexpr int kImageBytes = 2 * kB1Bytes + 2 * kB3Bytes + (kTw1 + kTw2 + kTw3) * 8;
+static_assert(kImageBytes % 16 == 0, "image copied in 16-byte pieces");
+constexpr float kStage2Scale = 1.0f / 32.0f;
+constexpr uint32_t kTmemCols = 256;
+
+// shared memory (bytes)
+constexpr int OFF_X0 = 0;                 // int8 frame, buffer 0 (32 KB)
+constexpr int OFF_X1 = 2 * kM;            // buffer 1
+constexpr int OFF_A = 4 * kM;             // operand A of stages 1 and 3 (64 KB)
+constexpr int OFF_AY = OFF_A + 65536;     // operand A of stage 2 (64 KB)
+constexpr int OFF_IMG = OFF_AY + 65536;   // B1 hi, B1 lo, B3 hi, B3 lo, tw1, tw2, tw3
+constexpr int OFF_B1H = OFF_IMG;
+constexpr int OFF_B1L = OFF_B1H + kB1Bytes;
+constexpr int OFF_B3H = OFF_B1L + kB1Bytes;
+constexpr int OFF_B3L = OFF_B3H + kB3Bytes;
+constexpr int OFF_TW1 = OFF_B3L + kB3Bytes;
+constexpr int OFF_TW2 = OFF_TW1 + kTw1 * 8;
+constexpr int OFF_TW3 = OFF_TW2 + kTw2 * 8;
+constexpr int OFF_BAR = OFF_IMG + kImageBytes;   // frame[2], MMA tile groups [4]
+constexpr int OFF_MISC = OFF_BAR + 48;           // TMEM base, abort flag
+constexpr int kSmem = OFF_MISC + 16;
+static_assert(OFF_A % 1024 == 0 && OFF_AY % 1024 == 0 && OFF_IMG % 16 == 0 && OFF_BAR % 16 == 0,
+              "alignment");
+static_assert(kSmem <= 227 * 1024, "shared memory");
+
+// --- row orders (a numpy model of these maps checks the whole transform) ---
+
+// Stage-1 row r1 = 128 t + 32 q + l holds b = 16 c + d with
+// d = (l & 7) + 8 ((4t+q) & 1), c = (l >> 3) + 4 ((4t+q) >> 1).
+__host__ __device__ __forceinline__ int b_of_r1(int r1) {
+    const int g = r1 >> 5, l = r1 & 31;
+    return 16 * ((l >> 3) + 4 * (g >> 1)) + (l & 7) + 8 * (g & 1);
+}
+// Stage-2 row of (k1, d): 32 (k1 >> 1) + 16 (k1 & 1) + d.
+__host__ __device__ __forceinline__ int r2_of(int k1, int d) {
+    return 32 * (k1 >> 1) + 16 * (k1 & 1) + d;
+}
+// Stage-3 row of (k1, k2a): k1 + 32 k2a for k2a < 16; the other half holds the
+// rows of Z[M-k] in the same lane of the tile four further on.
+__host__ __device__ __forceinline__ int r3_of(int k1, int k2a) {
+    if (k2a < 16) return k1 + 32 * k2a;
+    if (k1 == 0) return 512 + 32 * (k2a == 16 ? 0 : 32 - k2a);
+    return 512 + (32 - k1) + 32 * (31 - k2a);
+}
+// Byte offset of complex element e of row r in an operand with `sbo`.
+__host__ __device__ __forceinline__ uint32_t a_off(int r, int e, int sbo) {
+    return static_cast<uint32_t>((r >> 3) * sbo + (e >> 2) * kLBO + (r & 7) * 16 + (e & 3) * 4);
+}
+// Byte offset of element (n, k) of a B operand (N rows, K-major) with `sbo`.
+__host__ __device__ __forceinline__ uint32_t b_off(int n, int k, int sbo) {
+    return static_cast<uint32_t>((n >> 3) * sbo + (k >> 3) * kLBO + (n & 7) * 16 + (k & 7) * 2);
+}
+
+// --- tcgen05 wrappers ---
+
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, int sbo) {
+    // K-major, no swizzle: start>>4 | LBO>>4 << 16 | SBO>>4 << 32 | version 1 << 46
+    return static_cast<uint64_t>((addr >> 4) & 0x3FFFu) |
+           (static_cast<uint64_t>((kLBO >> 4) & 0x3FFF) << 16) |
+           (static_cast<uint64_t>((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ uint32_t idesc_f16(int m, int n) {
+    // D = F32, A = B = F16, both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+    return (1u << 4) | (static_cast<uint32_t>(n >> 3) << 17) |
+           (static_cast<uint32_t>(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                    uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *r) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_ld() {
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Two signed bytes -> FP16 pair, exactly: the biased bytes (b + 128) become the
+// low mantissa bits of 1024 (0x6400), and 1152 is subtracted.
+__device__ __forceinline__ uint32_t int8_pair_to_half2(uint32_t u16) {
+    const uint32_t x = u16 ^ 0x8080u;
+    const uint32_t h = __byte_perm(x, 0x64646464u, 0x4140);
+    const __half2 v = __hsub2(*reinterpret_cast<const __half2 *>(&h),
+                              __floats2half2_rn(1152.0f, 1152.0f));
+    return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+__device__ __forceinline__ void put_half2(unsigned char *base, uint32_t off, float2 v) {
+    *reinterpret_cast<__half2 *>(base + off) = __floats2half2_rn(v.x, v.y);
+}
+
+// Stage 1 or 2, one of four 128-row tiles: D = A (128 x 64) . B^T (64 x 64) at
+// columns 64 t, the hi and lo parts of B into one accumulator. Each tile is
+// committed to its own barrier, so its epilogue starts while the next tile's
+// MMAs run.
+__device__ __forceinline__ void issue_dft32(uint32_t tmem, uint32_t a, uint32_t bh, uint32_t bl,
+                                            uint64_t *bars) {
+    const uint32_t id = idesc_f16(128, 64);
+#pragma unroll 1
+    for (int t = 0; t < 4; ++t) {
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {
+            const uint64_t da = sdesc(a + t * 16 * kSboA12 + ks * 2 * kLBO, kSboA12);
+            mma(tmem + 64 * t, da, sdesc(bh + ks * 2 * kLBO, kSboB1), id, ks > 0 ? 1u : 0u);
+            mma(tmem + 64 * t, da, sdesc(bl + ks * 2 * kLBO, kSboB1), id, 1u);
+        }
+        mma_commit(&bars[t]);
+    }
+}
+
+// Stage 3: tiles t and t + 4 (the rows of Z[k] and of Z[M-k]) per barrier t,
+// D = A (128 x 32) . B^T (32 x 32) at columns 32 t.
+__device__ __forceinline__ void issue_dft16(uint32_t tmem, uint32_t a, uint32_t bh, uint32_t bl,
+                                            uint64_t *bars) {
+    const uint32_t id = idesc_f16(128, 32);
+#pragma unroll 1
+    for (int t = 0; t < 4; ++t) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int tt = t + 4 * h;
+#pragma unroll
+            for (int ks = 0; ks < 2; ++ks) {
+                const uint64_t da = sdesc(a + tt * 16 * kSboA3 + ks * 2 * kLBO, kSboA3);
+                mma(tmem + 32 * tt, da, sdesc(bh + ks * 2 * kLBO, kSboB3), id, ks > 0 ? 1u : 0u);
+                mma(tmem + 32 * tt, da, sdesc(bl + ks * 2 * kLBO, kSboB3), id, 1u);
+            }
+        }
+        mma_commit(&bars[t]);
+    }
+}
+
+template <bool CONTIG>
+__global__ void __launch_bounds__(kThreads, 1)
+    fengine_tc_kernel(FengineArgs a, const uint4 *__restrict__ image) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char *const sA = smem + OFF_A;
+    unsigned char *const sAY = smem + OFF_AY;
+    const float2 *tw1 = reinterpret_cast<const float2 *>(smem + OFF_TW1);
+    const float2 *tw2 = reinterpret_cast<const float2 *>(smem + OFF_TW2);
+    const float2 *tw3 = reinterpret_cast<const float2 *>(smem + OFF_TW3);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + OFF_BAR);   // [0], [1] frames
+    uint64_t *mbar = bar + 2;                                        // [4] MMA tile groups
+    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(smem + OFF_MISC);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + OFF_MISC + 4);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    {
+        uint4 *dst = reinterpret_cast<uint4 *>(smem + OFF_IMG);
+        for (int i = tid; i < kImageBytes / 16; i += kThreads) dst[i] = image[i];
+    }
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        for (int t = 0; t < 4; ++t) mbar_init(&mbar[t], 1);
+        *abort_flag = 0;
+        fence_mbar_init();
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_addr(s_tmem)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_before();
+    __syncthreads();
+    tc_after();
+    const uint32_t tmem = *s_tmem;
+    const uint32_t a_addr = smem_addr(sA), ay_addr = smem_addr(sAY);
+    const int my_tile = warp >> 2;   // the tile (group) whose epilogue this warp runs
+    const uint32_t lane_base = static_cast<uint32_t>(32 * (warp & 3)) << 16;
+
+    const int n_items = a.frames * a.n_station;
+    constexpr uint32_t frame_bytes = 2u * kM;
+    const int ytile_shift = __ffs(a.ytile) - 1;
+    const float out_scale = a.y_scale * 32.0f;   // undo stage 2's 1/32
+    auto src_of = [&](int item) {
+        const int f = item / a.n_station;
+        const int s = item - f * a.n_station;
+        return a.samples + static_cast<size_t>(s) * a.station_stride +
+               static_cast<size_t>(f) * a.frame_stride;
+    };
+    auto present = [&](int item) {
+        const int f = item / a.n_station;
+        return frame_present<kM>(a, f, item - f * a.n_station);
+    };
+
+    int item = blockIdx.x;
+    if (tid == 0 && item < n_items && present(item)) {
+        mbar_arrive_expect_tx(&bar[0], frame_bytes);
+        bulk_copy_g2s(smem + OFF_X0, src_of(item), frame_bytes, &bar[0]);
+    }
+    uint32_t parity_bits = 0u;   // bit b = phase parity of frame barrier b
+    uint32_t mma_parity = 0u;
+    bool failed = false;
+
+    int copy_buf = -1;   // buffer of the next item's frame copy in flight (tid 0), or -1
+    // A warp waits for its own tile group's MMAs; a timeout sets the abort flag,
+    // which every thread reads after the barrier that ends the stage.
+    auto wait_tile = [&]() {
+        if (!mbar_wait_bounded(&mbar[my_tile], mma_parity, a.err, kErrFengineCopyTimeout,
+                               abort_flag))
+            *abort_flag = 1;
+        tc_after();
+    };
+    bool mma_pending = false;   // (tid 0) a stage's MMAs issued, not yet seen complete
+    uint32_t pending_parity = 0u;
+    auto issued = [&]() {
+        mma_pending = true;
+        pending_parity = mma_parity;
+    };
+    auto end_stage = [&]() -> bool {   // operand writes visible to the tensor cores
+        fence_proxy_async_smem();
+        tc_before();
+        __syncthreads();
+        mma_parity ^= 1u;
+        if (*abort_flag != 0) return false;
+        mma_pending = false;   // every tile group was waited for before the barrier
+        return true;
+    };
+
+    for (int n = 0; item < n_items; ++n, item += gridDim.x) {
+        const int buf = n & 1;
+        const int next = item + gridDim.x;
+        bool next_issued = false;
+        if (tid == 0 && next < n_items && present(next)) {
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&bar[buf ^ 1], frame_bytes);
+            bulk_copy_g2s(smem + (buf ? OFF_X0 : OFF_X1), src_of(next), frame_bytes,
+                          &bar[buf ^ 1]);
+            next_issued = true;
+        }
+        copy_buf = next_issued ? (buf ^ 1) : -1;
+        using Row = YRow<kSpectraF16, CONTIG>;
+        const Row yrow{reinterpret_cast<typename Row::T *>(a.y) + static_cast<size_t>(item) * a.ytile,
+                       static_cast<uint32_t>(a.y_frames) * a.n_station * a.ytile, ytile_shift,
+                       out_scale, 0.5f * out_scale};
+        if (!present(item)) {
+            for (int k = tid; k < kM; k += kThreads) yrow.put(k, make_float2(0.f, 0.f));
+            continue;
+        }
+        const unsigned char *sx = smem + (buf ? OFF_X1 : OFF_X0);
+        if (!mbar_wait_bounded(&bar[buf], (parity_bits >> buf) & 1u, a.err,
+                               kErrFengineCopyTimeout))
+            *abort_flag = 1;
+        parity_bits ^= 1u << buf;
+        if (a.pmask != nullptr) {
+            const int f = item / a.n_station;
+            const uint32_t kept = packets_kept<kM>(a, f, item - f * a.n_station);
+            if (kept != all_packets<kM>()) {
+                uint4 *x16 = reinterpret_cast<uint4 *>(const_cast<unsigned char *>(sx));
+                for (int i = tid; i < kM / 8; i += kThreads)
+                    if (!((kept >> (i >> 6)) & 1u)) x16[i] = make_uint4(0u, 0u, 0u, 0u);
+                __syncthreads();
+            }
+        }
+
+        // Stage-1 operand: row r1 (b), complex elements a = 0..31, four per
+        // 16-byte store; a quarter warp stores one whole core matrix.
+        {
+            const uint16_t *px = reinterpret_cast<const uint16_t *>(sx);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int idx = tid + kThreads * i;
+                const int j = idx >> 9, r1 = idx & 511;
+                const int b = b_of_r1(r1);
+                uint4 v;
+                v.x = int8_pair_to_half2(px[512 * (4 * j + 0) + b]);
+                v.y = int8_pair_to_half2(px[512 * (4 * j + 1) + b]);
+                v.z = int8_pair_to_half2(px[512 * (4 * j + 2) + b]);
+                v.w = int8_pair_to_half2(px[512 * (4 * j + 3) + b]);
+                *reinterpret_cast<uint4 *>(sA + (r1 >> 3) * kSboA12 + j * kLBO + (r1 & 7) * 16) = v;
+            }
+        }
+        fence_proxy_async_smem();
+        tc_before();
+        __syncthreads();
+        if (*abort_flag) {
+            failed = true;
+            break;
+        }
+        if (tid == 0) {
+            tc_after();
+            issue_dft32(tmem, a_addr, smem_addr(smem + OFF_B1H), smem_addr(smem + OFF_B1L), mbar);
+            issued();
+        }
+        wait_tile();
+
+        // Stage-1 epilogue: row b, outputs k1 -> * W_M^(b k1) -> stage-2 row (k1, d),
+        // element c, in the second operand buffer.
+        {
+            const int t = warp >> 2;
+            const int b = b_of_r1(128 * t + 32 * (warp & 3) + lane);
+            const int c = b >> 4, d = b & 15;
+            uint32_t v[64];
+            const uint32_t ta = tmem + lane_base + 64 * t;
+            tmem_ld16(ta, v);
+            tmem_ld16(ta + 16, v + 16);
+            tmem_ld16(ta + 32, v + 32);
+            tmem_ld16(ta + 48, v + 48);
+            tmem_wait_ld();
+            const float2 w = tw1[b];
+            float2 wk = make_float2(1.f, 0.f);
+#pragma unroll
+            for (int k1 = 0; k1 < 32; ++k1) {
+                float2 y = make_float2(__uint_as_float(v[2 * k1]), __uint_as_float(v[2 * k1 + 1]));
+                if (k1 > 0) {
+                    wk = cmul(wk, w);
+                    y = cmul(y, wk);
+                }
+                put_half2(sAY, a_off(r2_of(k1, d), c, kSboA12), y);
+            }
+        }
+        if (!end_stage()) {
+            failed = true;
+            break;
+        }
+        if (tid == 0) {
+            tc_after();
+            issue_dft32(tmem, ay_addr, smem_addr(smem + OFF_B1H), smem_addr(smem + OFF_B1L), mbar);
+            issued();
+        }
+        wait_tile();
+
+        // Stage-2 epilogue: row (k1, d), outputs k2a -> * W_512^(d k2a)/32 ->
+        // stage-3 row (k1, k2a), element d.
+        {
+            const int t = warp >> 2;
+            const int g = 4 * t + (warp & 3);
+            const int k1 = 2 * g + (lane >> 4), d = lane & 15;
+            uint32_t v[64];
+            const uint32_t ta = tmem + lane_base + 64 * t;
+            tmem_ld16(ta, v);
+            tmem_ld16(ta + 16, v + 16);
+            tmem_ld16(ta + 32, v + 32);
+            tmem_ld16(ta + 48, v + 48);
+            tmem_wait_ld();
+#pragma unroll
+            for (int k2a = 0; k2a < 32; ++k2a) {
+                const float2 y = cmul(
+                    make_float2(__uint_as_float(v[2 * k2a]), __uint_as_float(v[2 * k2a + 1])),
+                    tw2[k2a * 16 + d]);
+                put_half2(sA, a_off(r3_of(k1, k2a), d, kSboA3), y);
+            }
+        }
+        if (!end_stage()) {
+            failed = true;
+            break;
+        }
+        if (tid == 0) {
+            tc_after();
+            issue_dft16(tmem, a_addr, smem_addr(smem + OFF_B3H), smem_addr(smem + OFF_B3L), mbar);
+            issued();
+        }
+        wait_tile();
+
+        // Stage-3 epilogue: thread p (row k1 + 32 k2a = p, k2a < 16) holds Z[p + 1024 i]
+        // in a[i] and, in the partner row, Z[M - p - 1024 i] in b[15 - i]; the real
+        // split gives X at both. Thread 0's rows (0, 0) and (0, 16) pair with themselves.
+        {
+            const int t = warp >> 2;
+            const int p = 128 * t + 32 * (warp & 3) + lane;
+            uint32_t u[32], w[32];
+            tmem_ld16(tmem + lane_base + 32 * t, u);
+            tmem_ld16(tmem + lane_base + 32 * t + 16, u + 16);
+            tmem_ld16(tmem + lane_base + 32 * (t + 4), w);
+            tmem_ld16(tmem + lane_base + 32 * (t + 4) + 16, w + 16);
+            tmem_wait_ld();
+            float2 za[16], zb[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                za[i] = make_float2(__uint_as_float(u[2 * i]), __uint_as_float(u[2 * i + 1]));
+                zb[i] = make_float2(__uint_as_float(w[2 * i]), __uint_as_float(w[2 * i + 1]));
+            }
+            const bool t0 = (p == 0);
+            const float2 wp = tw3[p];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const float2 zmk = t0 ? za[(16 - i) & 15] : zb[15 - i];
+                split_store(za[i], zmk, mul_w32(wp, i), p + 1024 * i, kM, !(t0 && i == 0), yrow);
+            }
+            const int kB = t0 ? 512 : p + 8192;
+            const float2 wB = t0 ? tw3[512] : mul_w32(wp, 8);
+#pragma unroll
+            for (int i = 8; i < 16; ++i) {
+                const float2 zk = t0 ? zb[i - 8] : za[i];
+                const float2 zmk = t0 ? zb[23 - i] : zb[15 - i];
+                split_store(zk, zmk, mul_w32(wB, i - 8), kB + 1024 * (i - 8), kM, true, yrow);
+            }
+            if (t0) yrow.put(kM / 2, make_float2(za[8].x * out_scale, -za[8].y * out_scale));
+        }
+        // every tile group's MMAs were waited for by its warps: after this barrier
+        // the operand buffers and TMEM are free for the next item
+        if (!end_stage()) {
+            failed = true;
+            break;
+        }
+    }
+    if (failed && tid == 0) {
+        // let the copy and the MMAs still in flight finish before the CTA and
+        // its accumulators go (each wait bounded; the error is already recorded)
+        if (copy_buf >= 0)
+            mbar_wait_bounded(&bar[copy_buf], (parity_bits >> copy_buf) & 1u, nullptr, 0);
+        if (mma_pending)   // the last tile group's commit covers all of the stage's MMAs
+            mbar_wait_bounded(&mbar[3], pending_parity, nullptr, 0);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        tc_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(kTmemCols)
+                     : "memory");
+    }
+}
+
+template <bool CONTIG>
+corr_status launch(const FengineArgs &a, const void *image, int num_sms, cudaStream_t stream) {
+    static bool configured = false;
+    if (!configured) {
+        corr_status st = cuda_check(
+            cudaFuncSetAttribute(fengine_tc_kernel<CONTIG>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem),
+            "cudaFuncSetAttribute(fengine_tc)");
+        if (st != CORR_OK) return st;
+        configured = true;
+    }
+    const int items = a.frames * a.n_station;
+    if (items <= 0) return CORR_OK;
+    const int grid = items < num_sms ? items : num_sms;
+    fengine_tc_kernel<CONTIG><<<grid, kThreads, kSmem, stream>>>(
+        a, static_cast<const uint4 *>(image));
+    return cuda_check(cudaGetLastError(), "fengine_tc_kernel launch");
+}
+
+} // namespace
+
+corr_status fengine_tc_prepare(void **d_image) {
+    *d_image = nullptr;
+    const double pi = 3.14159265358979323846;
+    std::vector<unsigned char> img(kImageBytes, 0);
+    auto put_half = [&](size_t off, double v) {
+        const __half h = __float2half_rn(static_cast<float>(v));
+        std::memcpy(&img[off], &h, 2);
+    };
+    // B = the real 2R x 2R form of the DFT-R matrix, rows n = 2k + (0 re, 1 im),
+    // columns (K) 2a + (0 re, 1 im): [[cos, sin], [-sin, cos]] of 2 pi a k / R.
+    auto build = [&](int R, size_t off_hi, size_t off_lo, int sbo) {
+        for (int n = 0; n < 2 * R; ++n)
+            for (int k = 0; k < 2 * R; ++k) {
+                const double th = 2.0 * pi * static_cast<double>((k >> 1) * (n >> 1)) / R;
+                const double c = std::cos(th), s = std::sin(th);
+                const double v = (n & 1) == 0 ? ((k & 1) == 0 ? c : s) : ((k & 1) == 0 ? -s : c);
+                const __half hi = __float2half_rn(static_cast<float>(v));
+                const double lo = v - static_cast<double>(__half2float(hi));
+                const size_t o = b_off(n, k, sbo);
+                std::memcpy(&img[off_hi + o], &hi, 2);
+                put_half(off_lo + o, lo);
+            }
+    };
+    build(32, OFF_B1H - OFF_IMG, OFF_B1L - OFF_IMG, kSboB1);
+    build(16, OFF_B3H - OFF_IMG, OFF_B3L - OFF_IMG, kSboB3);
+    auto put_c = [&](size_t off, double re, double im) {
+        const float2 v = make_float2(static_cast<float>(re), static_cast<float>(im));
+        std::memcpy(&img[off], &v, 8);
+    };
+    for (int b = 0; b < kTw1; ++b) {
+        const double th = -2.0 * pi * b / kM;
+        put_c(OFF_TW1 - OFF_IMG + 8 * b, std::cos(th), std::sin(th));
+    }
+    for (int k2a = 0; k2a < 32; ++k2a)
+        for (int d = 0; d < 16; ++d) {
+            const double th = -2.0 * pi * d * k2a / 512.0;
+            put_c(OFF_TW2 - OFF_IMG + 8 * (k2a * 16 + d), kStage2Scale * std::cos(th),
+                  kStage2Scale * std::sin(th));
+        }
+    for (int k = 0; k < kTw3; ++k) {
+        const double th = -2.0 * pi * k / (2.0 * kM);
+        put_c(OFF_TW3 - OFF_IMG + 8 * k, std::cos(th), std::sin(th));
+    }
+    void *d = nullptr;
+    corr_status st = cuda_check(cudaMalloc(&d, kImageBytes), "cudaMalloc(tensor FFT tables)");
+    if (st != CORR_OK) return st;
+    st = cuda_check(cudaMemcpy(d, img.data(), kImageBytes, cudaMemcpyHostToDevice),
+                    "cudaMemcpy(tensor FFT tables)");
+    if (st != CORR_OK) {
+        cudaFree(d);
+        return st;
+    }
+    *d_image = d;
+    return CORR_OK;
+}
+
+corr_status fengine_tc_launch(const FengineArgs &a, const void *image, int num_sms,
+                              cudaStream_t stream) {
+    if (image == nullptr) return fail(CORR_ERR_INTERNAL, "tensor FFT tables not prepared");
+    if (a.y_fmt != kSpectraF16)
+        return fail(CORR_ERR_ARG, "FFT plan 2 writes FP16 spectra only (the FP16 tensor X-engine)");
+    return a.ytile == kM ? launch<true>(a, image, num_sms, stream)
+                         : launch<false>(a, image, num_sms, stream);
+}
+
+} // namespace corrgb

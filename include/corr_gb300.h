@@ -102,8 +102,10 @@ typedef struct corrx_tiles {
     int32_t  ytile;
     int32_t  xct;
     int32_t  xkt;
-    int32_t  fplan;       /* F-engine FFT radix plan: 0 (three passes), or 1 at
-                             n_freq 16384 (four passes, twice the threads)        */
+    int32_t  fplan;       /* F-engine FFT plan: 0 (three passes), or at n_freq
+                             16384 also 1 (four passes, twice the threads) and,
+                             with FP16 spectra (CORR_X_TC_FP16) only, 2 (the
+                             DFT stages as tcgen05 matrix products)              */
     float    ms_fengine;  /* corrx_autotune: F-engine ms per max_frames pass       */
     float    ms_xengine;  /* corrx_autotune: X-engine ms per max_frames pass       */
 } corrx_tiles;
