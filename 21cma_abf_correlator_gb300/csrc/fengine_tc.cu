@@ -62,13 +62,15 @@ constexpr int kTw3 = 520;                 // exp(-2 pi i k / L), k <= 512
 constexpr int kImageBytes = 2 * kB1Bytes + 2 * kB3Bytes + (kTw1 + kTw2 + kTw3) * 8;
 static_assert(kImageBytes % 16 == 0, "image copied in 16-byte pieces");
 constexpr float kStage2Scale = 1.0f / 32.0f;
-constexpr uint32_t kTmemCols = 256;
+constexpr int kGroup = 256;               // threads per warp group
+constexpr uint32_t kTmemPerGroup = 256;
+constexpr uint32_t kTmemCols = 2 * kTmemPerGroup;
 
 // shared memory (bytes)
-constexpr int OFF_X0 = 0;                 // int8 frame, buffer 0 (32 KB)
-constexpr int OFF_X1 = 2 * kM;            // buffer 1
-constexpr int OFF_A = 4 * kM;             // operand A of stages 1 and 3 (64 KB)
-constexpr int OFF_AY = OFF_A + 65536;     // operand A of stage 2 (64 KB)
+constexpr int OFF_X0 = 0;                 // int8 frame of warp group 0 (32 KB)
+constexpr int OFF_X1 = 2 * kM;            // warp group 1
+constexpr int OFF_A = 4 * kM;             // stage operand of warp group 0 (64 KB)
+constexpr int OFF_AY = OFF_A + 65536;     // warp group 1
 constexpr int OFF_IMG = OFF_AY + 65536;   // B1 hi, B1 lo, B3 hi, B3 lo, tw1, tw2, tw3
 constexpr int OFF_B1H = OFF_IMG;
 constexpr int OFF_B1L = OFF_B1H + kB1Bytes;
@@ -77,7 +79,7 @@ constexpr int OFF_B3L = OFF_B3H + kB3Bytes;
 constexpr int OFF_TW1 = OFF_B3L + kB3Bytes;
 constexpr int OFF_TW2 = OFF_TW1 + kTw1 * 8;
 constexpr int OFF_TW3 = OFF_TW2 + kTw2 * 8;
-constexpr int OFF_BAR = OFF_IMG + kImageBytes;   // frame[2], MMA tile groups [4]
+constexpr int OFF_BAR = OFF_IMG + kImageBytes;   // frame[2], MMA[2] (one each per group)
 constexpr int OFF_MISC = OFF_BAR + 48;           // TMEM base, abort flag
 constexpr int kSmem = OFF_MISC + 16;
 static_assert(OFF_A % 1024 == 0 && OFF_AY % 1024 == 0 && OFF_IMG % 16 == 0 && OFF_BAR % 16 == 0,
@@ -177,16 +179,13 @@ __device__ __forceinline__ uint32_t int8_pair_to_half2(uint32_t u16) {
     return *reinterpret_cast<const uint32_t *>(&v);
 }
 
-__device__ __forceinline__ void put_half2(unsigned char *base, uint32_t off, float2 v) {
+__device__ __forceinline__ void put_half2(unsigned char *base, int off, float2 v) {
     *reinterpret_cast<__half2 *>(base + off) = __floats2half2_rn(v.x, v.y);
 }
 
-// Stage 1 or 2, one of four 128-row tiles: D = A (128 x 64) . B^T (64 x 64) at
-// columns 64 t, the hi and lo parts of B into one accumulator. Each tile is
-// committed to its own barrier, so its epilogue starts while the next tile's
-// MMAs run.
-__device__ __forceinline__ void issue_dft32(uint32_t tmem, uint32_t a, uint32_t bh, uint32_t bl,
-                                            uint64_t *bars) {
+// Stage 1 or 2: four 128-row tiles, D = A (128 x 64) . B^T (64 x 64) at columns
+// 64 t, the hi and lo parts of B into one accumulator per tile.
+__device__ __forceinline__ void issue_dft32(uint32_t tmem, uint32_t a, uint32_t bh, uint32_t bl) {
     const uint32_t id = idesc_f16(128, 64);
 #pragma unroll 1
     for (int t = 0; t < 4; ++t) {
@@ -196,54 +195,47 @@ __device__ __forceinline__ void issue_dft32(uint32_t tmem, uint32_t a, uint32_t 
             mma(tmem + 64 * t, da, sdesc(bh + ks * 2 * kLBO, kSboB1), id, ks > 0 ? 1u : 0u);
             mma(tmem + 64 * t, da, sdesc(bl + ks * 2 * kLBO, kSboB1), id, 1u);
         }
-        mma_commit(&bars[t]);
     }
 }
 
-// Stage 3: tiles t and t + 4 (the rows of Z[k] and of Z[M-k]) per barrier t,
-// D = A (128 x 32) . B^T (32 x 32) at columns 32 t.
-__device__ __forceinline__ void issue_dft16(uint32_t tmem, uint32_t a, uint32_t bh, uint32_t bl,
-                                            uint64_t *bars) {
+// Stage 3: eight 128-row tiles, D = A (128 x 32) . B^T (32 x 32) at columns 32 t.
+__device__ __forceinline__ void issue_dft16(uint32_t tmem, uint32_t a, uint32_t bh, uint32_t bl) {
     const uint32_t id = idesc_f16(128, 32);
 #pragma unroll 1
-    for (int t = 0; t < 4; ++t) {
+    for (int t = 0; t < 8; ++t) {
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int tt = t + 4 * h;
-#pragma unroll
-            for (int ks = 0; ks < 2; ++ks) {
-                const uint64_t da = sdesc(a + tt * 16 * kSboA3 + ks * 2 * kLBO, kSboA3);
-                mma(tmem + 32 * tt, da, sdesc(bh + ks * 2 * kLBO, kSboB3), id, ks > 0 ? 1u : 0u);
-                mma(tmem + 32 * tt, da, sdesc(bl + ks * 2 * kLBO, kSboB3), id, 1u);
-            }
+        for (int ks = 0; ks < 2; ++ks) {
+            const uint64_t da = sdesc(a + t * 16 * kSboA3 + ks * 2 * kLBO, kSboA3);
+            mma(tmem + 32 * t, da, sdesc(bh + ks * 2 * kLBO, kSboB3), id, ks > 0 ? 1u : 0u);
+            mma(tmem + 32 * t, da, sdesc(bl + ks * 2 * kLBO, kSboB3), id, 1u);
         }
-        mma_commit(&bars[t]);
     }
 }
 
+// Two warp groups of 256 threads share the SM, each carrying its own items
+// through the three stages with its own frame buffer, operand buffer, 256 TMEM
+// columns and barriers (named barrier 1 + group): while one group runs an
+// epilogue on the CUDA cores, the other's MMAs run on the tensor cores.
 template <bool CONTIG>
 __global__ void __launch_bounds__(kThreads, 1)
     fengine_tc_kernel(FengineArgs a, const uint4 *__restrict__ image) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *const sA = smem + OFF_A;
-    unsigned char *const sAY = smem + OFF_AY;
     const float2 *tw1 = reinterpret_cast<const float2 *>(smem + OFF_TW1);
     const float2 *tw2 = reinterpret_cast<const float2 *>(smem + OFF_TW2);
     const float2 *tw3 = reinterpret_cast<const float2 *>(smem + OFF_TW3);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + OFF_BAR);   // [0], [1] frames
-    uint64_t *mbar = bar + 2;                                        // [4] MMA tile groups
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + OFF_BAR);   // frame[2], MMA[2]
     uint32_t *s_tmem = reinterpret_cast<uint32_t *>(smem + OFF_MISC);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + OFF_MISC + 4);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int grp = warp >> 3, gtid = tid & (kGroup - 1);
+    const int q = warp & 3, th = (warp >> 2) & 1;   // TMEM lane quarter; tiles th, th + 2
     {
         uint4 *dst = reinterpret_cast<uint4 *>(smem + OFF_IMG);
         for (int i = tid; i < kImageBytes / 16; i += kThreads) dst[i] = image[i];
     }
     if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-        for (int t = 0; t < 4; ++t) mbar_init(&mbar[t], 1);
+        for (int i = 0; i < 4; ++i) mbar_init(&bar[i], 1);
         *abort_flag = 0;
         fence_mbar_init();
     }
@@ -257,93 +249,87 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc_before();
     __syncthreads();
     tc_after();
-    const uint32_t tmem = *s_tmem;
-    const uint32_t a_addr = smem_addr(sA), ay_addr = smem_addr(sAY);
-    const int my_tile = warp >> 2;   // the tile (group) whose epilogue this warp runs
-    const uint32_t lane_base = static_cast<uint32_t>(32 * (warp & 3)) << 16;
+    const uint32_t tmem = *s_tmem + kTmemPerGroup * grp;
+    unsigned char *const sA = smem + (grp ? OFF_AY : OFF_A);
+    unsigned char *const sx = smem + (grp ? OFF_X1 : OFF_X0);
+    uint64_t *const fbar = &bar[grp];
+    uint64_t *const mbar = &bar[2 + grp];
+    const uint32_t a_addr = smem_addr(sA);
+    const uint32_t lane_base = static_cast<uint32_t>(32 * q) << 16;
+    auto group_sync = [&]() { asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "n"(kGroup) : "memory"); };
 
     const int n_items = a.frames * a.n_station;
+    const int stride = 2 * static_cast<int>(gridDim.x);
     constexpr uint32_t frame_bytes = 2u * kM;
     const int ytile_shift = __ffs(a.ytile) - 1;
     const float out_scale = a.y_scale * 32.0f;   // undo stage 2's 1/32
-    auto src_of = [&](int item) {
-        const int f = item / a.n_station;
-        const int s = item - f * a.n_station;
+    auto src_of = [&](int it) {
+        const int f = it / a.n_station;
+        const int s = it - f * a.n_station;
         return a.samples + static_cast<size_t>(s) * a.station_stride +
                static_cast<size_t>(f) * a.frame_stride;
     };
-    auto present = [&](int item) {
-        const int f = item / a.n_station;
-        return frame_present<kM>(a, f, item - f * a.n_station);
+    auto present = [&](int it) {
+        const int f = it / a.n_station;
+        return frame_present<kM>(a, f, it - f * a.n_station);
+    };
+    bool copy_pending = false;   // (gtid 0) a frame copy into this group's buffer
+    auto fetch = [&](int it) {   // gtid 0: request item it's frame if it has one
+        if (it < n_items && present(it)) {
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(fbar, frame_bytes);
+            bulk_copy_g2s(sx, src_of(it), frame_bytes, fbar);
+            copy_pending = true;
+        }
     };
 
-    int item = blockIdx.x;
-    if (tid == 0 && item < n_items && present(item)) {
-        mbar_arrive_expect_tx(&bar[0], frame_bytes);
-        bulk_copy_g2s(smem + OFF_X0, src_of(item), frame_bytes, &bar[0]);
-    }
-    uint32_t parity_bits = 0u;   // bit b = phase parity of frame barrier b
-    uint32_t mma_parity = 0u;
+    int item = 2 * static_cast<int>(blockIdx.x) + grp;
+    if (gtid == 0) fetch(item);
+    uint32_t fpar = 0u, mpar = 0u;
+    bool mma_pending = false;     // (gtid 0) MMAs issued, completion not yet seen
+    uint32_t pending_par = 0u;    // the phase their completion ends
     bool failed = false;
 
-    int copy_buf = -1;   // buffer of the next item's frame copy in flight (tid 0), or -1
-    // A warp waits for its own tile group's MMAs; a timeout sets the abort flag,
-    // which every thread reads after the barrier that ends the stage.
-    auto wait_tile = [&]() {
-        if (!mbar_wait_bounded(&mbar[my_tile], mma_parity, a.err, kErrFengineCopyTimeout,
-                               abort_flag))
+    auto issued = [&]() {
+        mma_commit(mbar);
+        mma_pending = true;
+        pending_par = mpar;
+    };
+    auto wait_mma = [&]() {
+        if (!mbar_wait_bounded(mbar, mpar, a.err, kErrFengineCopyTimeout, abort_flag))
             *abort_flag = 1;
         tc_after();
     };
-    bool mma_pending = false;   // (tid 0) a stage's MMAs issued, not yet seen complete
-    uint32_t pending_parity = 0u;
-    auto issued = [&]() {
-        mma_pending = true;
-        pending_parity = mma_parity;
-    };
-    auto end_stage = [&]() -> bool {   // operand writes visible to the tensor cores
+    // End of a phase: operand writes visible to the tensor cores, TMEM reads
+    // done, the group in step; the abort flag is read after the barrier.
+    auto end_phase = [&]() -> bool {
         fence_proxy_async_smem();
         tc_before();
-        __syncthreads();
-        mma_parity ^= 1u;
-        if (*abort_flag != 0) return false;
-        mma_pending = false;   // every tile group was waited for before the barrier
-        return true;
+        group_sync();
+        return *abort_flag == 0;
     };
 
-    for (int n = 0; item < n_items; ++n, item += gridDim.x) {
-        const int buf = n & 1;
-        const int next = item + gridDim.x;
-        bool next_issued = false;
-        if (tid == 0 && next < n_items && present(next)) {
-            fence_proxy_async_smem();
-            mbar_arrive_expect_tx(&bar[buf ^ 1], frame_bytes);
-            bulk_copy_g2s(smem + (buf ? OFF_X0 : OFF_X1), src_of(next), frame_bytes,
-                          &bar[buf ^ 1]);
-            next_issued = true;
-        }
-        copy_buf = next_issued ? (buf ^ 1) : -1;
+    for (; item < n_items; item += stride) {
         using Row = YRow<kSpectraF16, CONTIG>;
         const Row yrow{reinterpret_cast<typename Row::T *>(a.y) + static_cast<size_t>(item) * a.ytile,
                        static_cast<uint32_t>(a.y_frames) * a.n_station * a.ytile, ytile_shift,
                        out_scale, 0.5f * out_scale};
         if (!present(item)) {
-            for (int k = tid; k < kM; k += kThreads) yrow.put(k, make_float2(0.f, 0.f));
+            for (int k = gtid; k < kM; k += kGroup) yrow.put(k, make_float2(0.f, 0.f));
+            if (gtid == 0) fetch(item + stride);
             continue;
         }
-        const unsigned char *sx = smem + (buf ? OFF_X1 : OFF_X0);
-        if (!mbar_wait_bounded(&bar[buf], (parity_bits >> buf) & 1u, a.err,
-                               kErrFengineCopyTimeout))
+        if (!mbar_wait_bounded(fbar, fpar, a.err, kErrFengineCopyTimeout, abort_flag))
             *abort_flag = 1;
-        parity_bits ^= 1u << buf;
+        fpar ^= 1u;
         if (a.pmask != nullptr) {
             const int f = item / a.n_station;
             const uint32_t kept = packets_kept<kM>(a, f, item - f * a.n_station);
             if (kept != all_packets<kM>()) {
-                uint4 *x16 = reinterpret_cast<uint4 *>(const_cast<unsigned char *>(sx));
-                for (int i = tid; i < kM / 8; i += kThreads)
+                uint4 *x16 = reinterpret_cast<uint4 *>(sx);
+                for (int i = gtid; i < kM / 8; i += kGroup)
                     if (!((kept >> (i >> 6)) & 1u)) x16[i] = make_uint4(0u, 0u, 0u, 0u);
-                __syncthreads();
+                group_sync();
             }
         }
 
@@ -351,9 +337,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         // 16-byte store; a quarter warp stores one whole core matrix.
         {
             const uint16_t *px = reinterpret_cast<const uint16_t *>(sx);
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int idx = tid + kThreads * i;
+#pragma unroll 4
+            for (int i = 0; i < 16; ++i) {
+                const int idx = gtid + kGroup * i;
                 const int j = idx >> 9, r1 = idx & 511;
                 const int b = b_of_r1(r1);
                 uint4 v;
@@ -364,100 +350,123 @@ __global__ void __launch_bounds__(kThreads, 1)
                 *reinterpret_cast<uint4 *>(sA + (r1 >> 3) * kSboA12 + j * kLBO + (r1 & 7) * 16) = v;
             }
         }
-        fence_proxy_async_smem();
-        tc_before();
-        __syncthreads();
-        if (*abort_flag) {
+        if (!end_phase()) {
             failed = true;
             break;
         }
-        if (tid == 0) {
+        if (gtid == 0) {
+            copy_pending = false;    // landed and read
+            fetch(item + stride);    // the group's next frame, into the buffer just read
             tc_after();
-            issue_dft32(tmem, a_addr, smem_addr(smem + OFF_B1H), smem_addr(smem + OFF_B1L), mbar);
+            issue_dft32(tmem, a_addr, smem_addr(smem + OFF_B1H), smem_addr(smem + OFF_B1L));
             issued();
         }
-        wait_tile();
+        wait_mma();
+        mpar ^= 1u;
 
-        // Stage-1 epilogue: row b, outputs k1 -> * W_M^(b k1) -> stage-2 row (k1, d),
-        // element c, in the second operand buffer.
-        {
-            const int t = warp >> 2;
-            const int b = b_of_r1(128 * t + 32 * (warp & 3) + lane);
+        // Stage-1 epilogue: row b, outputs k1 -> * W_M^(b k1) -> stage-2 row (k1, d), element c.
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+            const int t = th + 2 * h;
+            const int b = b_of_r1(128 * t + 32 * q + lane);
             const int c = b >> 4, d = b & 15;
             uint32_t v[64];
             const uint32_t ta = tmem + lane_base + 64 * t;
             tmem_ld16(ta, v);
             tmem_ld16(ta + 16, v + 16);
-            tmem_ld16(ta + 32, v + 32);
-            tmem_ld16(ta + 48, v + 48);
             tmem_wait_ld();
+            tmem_ld16(ta + 32, v + 32);   // lands while the first half is worked
+            tmem_ld16(ta + 48, v + 48);
             const float2 w = tw1[b];
             float2 wk = make_float2(1.f, 0.f);
+            unsigned char *const dst = sA + a_off(r2_of(0, d), c, kSboA12);
 #pragma unroll
             for (int k1 = 0; k1 < 32; ++k1) {
+                if (k1 == 16) tmem_wait_ld();
                 float2 y = make_float2(__uint_as_float(v[2 * k1]), __uint_as_float(v[2 * k1 + 1]));
                 if (k1 > 0) {
                     wk = cmul(wk, w);
                     y = cmul(y, wk);
                 }
-                put_half2(sAY, a_off(r2_of(k1, d), c, kSboA12), y);
+                // r2_of(k1, d) - r2_of(0, d) = 32 (k1 >> 1) + 16 (k1 & 1): whole 8-row groups
+                put_half2(dst, (4 * (k1 >> 1) + 2 * (k1 & 1)) * kSboA12, y);
             }
         }
-        if (!end_stage()) {
+        if (!end_phase()) {
             failed = true;
             break;
         }
-        if (tid == 0) {
+        if (gtid == 0) {
+            mma_pending = false;
             tc_after();
-            issue_dft32(tmem, ay_addr, smem_addr(smem + OFF_B1H), smem_addr(smem + OFF_B1L), mbar);
+            issue_dft32(tmem, a_addr, smem_addr(smem + OFF_B1H), smem_addr(smem + OFF_B1L));
             issued();
         }
-        wait_tile();
+        wait_mma();
+        mpar ^= 1u;
 
         // Stage-2 epilogue: row (k1, d), outputs k2a -> * W_512^(d k2a)/32 ->
         // stage-3 row (k1, k2a), element d.
-        {
-            const int t = warp >> 2;
-            const int g = 4 * t + (warp & 3);
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+            const int t = th + 2 * h;
+            const int g = 4 * t + q;
             const int k1 = 2 * g + (lane >> 4), d = lane & 15;
             uint32_t v[64];
             const uint32_t ta = tmem + lane_base + 64 * t;
             tmem_ld16(ta, v);
             tmem_ld16(ta + 16, v + 16);
-            tmem_ld16(ta + 32, v + 32);
-            tmem_ld16(ta + 48, v + 48);
             tmem_wait_ld();
+            tmem_ld16(ta + 32, v + 32);   // lands while the first half is worked
+            tmem_ld16(ta + 48, v + 48);
+            // k2a < 16: rows k1 + 32 k2a (4 row groups apart per k2a). k2a >= 16:
+            // rows of the partner half, 4 groups back per k2a from k2a = 16, except
+            // that k1 = 0 at k2a = 16 is row 512.
+            unsigned char *const lo = sA + a_off(k1, d, kSboA3);
+            const uint32_t hi16 = a_off(r3_of(k1, 16), d, kSboA3);
+            const uint32_t hi17 = a_off(r3_of(k1, 17), d, kSboA3) + 4 * kSboA3;
+            unsigned char *const hi = sA + hi17;
 #pragma unroll
             for (int k2a = 0; k2a < 32; ++k2a) {
+                if (k2a == 16) tmem_wait_ld();
                 const float2 y = cmul(
                     make_float2(__uint_as_float(v[2 * k2a]), __uint_as_float(v[2 * k2a + 1])),
                     tw2[k2a * 16 + d]);
-                put_half2(sA, a_off(r3_of(k1, k2a), d, kSboA3), y);
+                if (k2a < 16)
+                    put_half2(lo, k2a * 4 * kSboA3, y);
+                else if (k2a == 16)
+                    put_half2(sA, static_cast<int>(hi16), y);
+                else
+                    put_half2(hi, -(k2a - 16) * 4 * kSboA3, y);
             }
         }
-        if (!end_stage()) {
+        if (!end_phase()) {
             failed = true;
             break;
         }
-        if (tid == 0) {
+        if (gtid == 0) {
+            mma_pending = false;
             tc_after();
-            issue_dft16(tmem, a_addr, smem_addr(smem + OFF_B3H), smem_addr(smem + OFF_B3L), mbar);
+            issue_dft16(tmem, a_addr, smem_addr(smem + OFF_B3H), smem_addr(smem + OFF_B3L));
             issued();
         }
-        wait_tile();
+        wait_mma();
+        mpar ^= 1u;
 
         // Stage-3 epilogue: thread p (row k1 + 32 k2a = p, k2a < 16) holds Z[p + 1024 i]
-        // in a[i] and, in the partner row, Z[M - p - 1024 i] in b[15 - i]; the real
-        // split gives X at both. Thread 0's rows (0, 0) and (0, 16) pair with themselves.
-        {
-            const int t = warp >> 2;
-            const int p = 128 * t + 32 * (warp & 3) + lane;
+        // in za[i] and, in the partner row, Z[M - p - 1024 i] in zb[15 - i]; the real
+        // split gives X at both. Row p = 0 ((0, 0)) and its partner (0, 16) pair
+        // with themselves.
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+            const int t = th + 2 * h;
+            const int p = 128 * t + 32 * q + lane;
             uint32_t u[32], w[32];
             tmem_ld16(tmem + lane_base + 32 * t, u);
             tmem_ld16(tmem + lane_base + 32 * t + 16, u + 16);
             tmem_ld16(tmem + lane_base + 32 * (t + 4), w);
             tmem_ld16(tmem + lane_base + 32 * (t + 4) + 16, w + 16);
-            tmem_wait_ld();
+            tmem_wait_ld();   // both rows feed every split below
             float2 za[16], zb[16];
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
@@ -481,25 +490,23 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             if (t0) yrow.put(kM / 2, make_float2(za[8].x * out_scale, -za[8].y * out_scale));
         }
-        // every tile group's MMAs were waited for by its warps: after this barrier
-        // the operand buffers and TMEM are free for the next item
-        if (!end_stage()) {
+        if (!end_phase()) {
             failed = true;
             break;
         }
+        if (gtid == 0) mma_pending = false;
     }
-    if (failed && tid == 0) {
-        // let the copy and the MMAs still in flight finish before the CTA and
-        // its accumulators go (each wait bounded; the error is already recorded)
-        if (copy_buf >= 0)
-            mbar_wait_bounded(&bar[copy_buf], (parity_bits >> copy_buf) & 1u, nullptr, 0);
-        if (mma_pending)   // the last tile group's commit covers all of the stage's MMAs
-            mbar_wait_bounded(&mbar[3], pending_parity, nullptr, 0);
+    if (failed && gtid == 0) {
+        // let this group's copy and MMAs in flight finish before the CTA and its
+        // accumulators go (each wait bounded; the error is already recorded)
+        if (copy_pending) mbar_wait_bounded(fbar, fpar, nullptr, 0);
+        if (mma_pending) mbar_wait_bounded(mbar, pending_par, nullptr, 0);
     }
     __syncthreads();
     if (warp == 0) {
         tc_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(
+                         *s_tmem),
                      "r"(kTmemCols)
                      : "memory");
     }
@@ -518,7 +525,8 @@ corr_status launch(const FengineArgs &a, const void *image, int num_sms, cudaStr
     }
     const int items = a.frames * a.n_station;
     if (items <= 0) return CORR_OK;
-    const int grid = items < num_sms ? items : num_sms;
+    const int pairs = (items + 1) / 2;   // each CTA carries two items at a time
+    const int grid = pairs < num_sms ? pairs : num_sms;
     fengine_tc_kernel<CONTIG><<<grid, kThreads, kSmem, stream>>>(
         a, static_cast<const uint4 *>(image));
     return cuda_check(cudaGetLastError(), "fengine_tc_kernel launch");
