@@ -282,6 +282,8 @@ SIGNATURES = {
     "corrx_frontend_fill": (C.c_int, [C.POINTER(corrx_frontend), C.c_int32, C.c_int32,
                                       C.c_int32, C.c_int64, C.c_int32, C.c_void_p, C.c_size_t, C.c_size_t,
                                       C.c_void_p, C.c_size_t, C.c_void_p]),
+    "corrx_tc_fft_maps": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p]),
     "corrx_accumulate_packets": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t,
                                            C.c_void_p, C.c_size_t, C.c_int32, C.c_void_p,
                                            C.c_size_t, C.c_int32, C.c_int32, C.c_void_p,

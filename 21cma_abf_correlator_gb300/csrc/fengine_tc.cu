@@ -590,6 +590,25 @@ corr_status fengine_tc_prepare(void **d_image) {
     return CORR_OK;
 }
 
+} // namespace corrgb
+
+extern "C" corr_status corrx_tc_fft_maps(int32_t *b_of_row, int32_t *row2, int32_t *row3,
+                                         uint32_t *off12, uint32_t *off3) {
+    using namespace corrgb;
+    for (int r = 0; b_of_row != nullptr && r < 512; ++r) b_of_row[r] = b_of_r1(r);
+    for (int k1 = 0; k1 < 32; ++k1) {
+        for (int d = 0; row2 != nullptr && d < 16; ++d) row2[k1 * 16 + d] = r2_of(k1, d);
+        for (int k2a = 0; row3 != nullptr && k2a < 32; ++k2a) row3[k1 * 32 + k2a] = r3_of(k1, k2a);
+    }
+    for (int r = 0; off12 != nullptr && r < 512; ++r)
+        for (int e = 0; e < 32; ++e) off12[r * 32 + e] = a_off(r, e, kSboA12);
+    for (int r = 0; off3 != nullptr && r < 1024; ++r)
+        for (int e = 0; e < 16; ++e) off3[r * 16 + e] = a_off(r, e, kSboA3);
+    return CORR_OK;
+}
+
+namespace corrgb {
+
 corr_status fengine_tc_launch(const FengineArgs &a, const void *image, int num_sms,
                               cudaStream_t stream) {
     if (image == nullptr) return fail(CORR_ERR_INTERNAL, "tensor FFT tables not prepared");

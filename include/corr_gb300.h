@@ -234,6 +234,20 @@ corr_status corrx_tc_geometry(int32_t n_station, int32_t split, int32_t ct, int3
                               corrx_tc_geom *out);
 
 /*
+ * The row orders and operand offsets of FFT plan 2 (the tensor-core F-engine at
+ * n_freq 16384), exactly as its kernel computes them; no device work. Fills
+ *   b_of_row[512]      stage-1 row -> b (n = 512 a + b)
+ *   row2[32 * 16]      [k1 * 16 + d] -> stage-2 row
+ *   row3[32 * 32]      [k1 * 32 + k2a] -> stage-3 row
+ *   off12[512 * 32]    [row * 32 + e] -> byte offset of complex element e of a
+ *                      stage-1/2 operand row
+ *   off3[1024 * 16]    [row * 16 + e] -> the same for the stage-3 operand
+ * (any pointer may be NULL to skip it).
+ */
+corr_status corrx_tc_fft_maps(int32_t *b_of_row, int32_t *row2, int32_t *row3, uint32_t *off12,
+                              uint32_t *off3);
+
+/*
  * On-device synthetic front end: the traffic of the reference's test transmitter
  * (corr-rs/src/bin/replay.rs), assembled into frames and a validity mask the way
  * the receive side does it (corr-rs/src/assemble.rs), written straight into
