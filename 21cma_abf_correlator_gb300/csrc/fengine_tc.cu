@@ -27,12 +27,15 @@
 // stage 3 stays in FP32. The spectrum goes out as FP16 pairs scaled by
 // y_scale (x32 to undo the 1/32), exactly as the CUDA-core F-engine writes them.
 //
-// One CTA per SM (168 KB of shared memory, 256 TMEM columns), persistent over
-// (frame, station) items like fengine.cu: the next item's int8 frame arrives by
-// a TMA bulk copy while the current one is transformed; missing frames and
-// lost packets are handled the same way. Within an item the stages run in
-// order: all warps convert, one thread issues the MMAs, all warps wait for them
-// (clock-bounded mbarrier waits) and run the epilogue.
+// One CTA per SM (229.5 KB of shared memory, 512 TMEM columns), persistent over
+// (frame, station) items like fengine.cu, with two warp groups of 256 threads
+// that each carry their own items: a group has its own int8 frame buffer (the
+// next item's frame arrives by a TMA bulk copy once the current one has been
+// read), its own 64 KB operand buffer, 256 TMEM columns, mbarriers and named
+// barrier. Within an item a group's stages run in order: its threads convert,
+// one of them issues the MMAs, all wait for them (clock-bounded mbarrier waits)
+// and run the epilogue; meanwhile the other group's MMAs or epilogue run.
+// Missing frames and lost packets are handled as in fengine.cu.
 
 #include <cmath>
 #include <cstring>
