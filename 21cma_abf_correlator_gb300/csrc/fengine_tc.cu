@@ -66,6 +66,7 @@ constexpr int kImageBytes = 2 * kB1Bytes + 2 * kB3Bytes + (kTw1 + kTw2 + kTw3) *
 static_assert(kImageBytes % 16 == 0, "image copied in 16-byte pieces");
 constexpr float kStage2Scale = 1.0f / 32.0f;
 constexpr int kGroup = 256;               // threads per warp group
+constexpr int kIssuers = 4;               // MMA-issuing threads per group (lane 0 of its first warps)
 constexpr uint32_t kTmemPerGroup = 256;
 constexpr uint32_t kTmemCols = 2 * kTmemPerGroup;
 
@@ -186,31 +187,32 @@ __device__ __forceinline__ void put_half2(unsigned char *base, int off, float2 v
     *reinterpret_cast<__half2 *>(base + off) = __floats2half2_rn(v.x, v.y);
 }
 
-// Stage 1 or 2: four 128-row tiles, D = A (128 x 64) . B^T (64 x 64) at columns
-// 64 t, the hi and lo parts of B into one accumulator per tile.
-__device__ __forceinline__ void issue_dft32(uint32_t tmem, uint32_t a, uint32_t bh, uint32_t bl) {
+// Stage 1 or 2, tile t of four: D = A (128 x 64) . B^T (64 x 64) at columns 64 t,
+// the hi and lo parts of B into one accumulator. Each of four threads issues one
+// tile (issuing many small MMAs from one thread is slower than the tensor cores).
+__device__ __forceinline__ void issue_dft32(uint32_t tmem, uint32_t a, uint32_t bh, uint32_t bl,
+                                            int t) {
     const uint32_t id = idesc_f16(128, 64);
-#pragma unroll 1
-    for (int t = 0; t < 4; ++t) {
 #pragma unroll
-        for (int ks = 0; ks < 4; ++ks) {
-            const uint64_t da = sdesc(a + t * 16 * kSboA12 + ks * 2 * kLBO, kSboA12);
-            mma(tmem + 64 * t, da, sdesc(bh + ks * 2 * kLBO, kSboB1), id, ks > 0 ? 1u : 0u);
-            mma(tmem + 64 * t, da, sdesc(bl + ks * 2 * kLBO, kSboB1), id, 1u);
-        }
+    for (int ks = 0; ks < 4; ++ks) {
+        const uint64_t da = sdesc(a + t * 16 * kSboA12 + ks * 2 * kLBO, kSboA12);
+        mma(tmem + 64 * t, da, sdesc(bh + ks * 2 * kLBO, kSboB1), id, ks > 0 ? 1u : 0u);
+        mma(tmem + 64 * t, da, sdesc(bl + ks * 2 * kLBO, kSboB1), id, 1u);
     }
 }
 
-// Stage 3: eight 128-row tiles, D = A (128 x 32) . B^T (32 x 32) at columns 32 t.
-__device__ __forceinline__ void issue_dft16(uint32_t tmem, uint32_t a, uint32_t bh, uint32_t bl) {
+// Stage 3, tiles t and t + 4 of eight: D = A (128 x 32) . B^T (32 x 32) at columns 32 t.
+__device__ __forceinline__ void issue_dft16(uint32_t tmem, uint32_t a, uint32_t bh, uint32_t bl,
+                                            int t) {
     const uint32_t id = idesc_f16(128, 32);
-#pragma unroll 1
-    for (int t = 0; t < 8; ++t) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int tt = t + 4 * h;
 #pragma unroll
         for (int ks = 0; ks < 2; ++ks) {
-            const uint64_t da = sdesc(a + t * 16 * kSboA3 + ks * 2 * kLBO, kSboA3);
-            mma(tmem + 32 * t, da, sdesc(bh + ks * 2 * kLBO, kSboB3), id, ks > 0 ? 1u : 0u);
-            mma(tmem + 32 * t, da, sdesc(bl + ks * 2 * kLBO, kSboB3), id, 1u);
+            const uint64_t da = sdesc(a + tt * 16 * kSboA3 + ks * 2 * kLBO, kSboA3);
+            mma(tmem + 32 * tt, da, sdesc(bh + ks * 2 * kLBO, kSboB3), id, ks > 0 ? 1u : 0u);
+            mma(tmem + 32 * tt, da, sdesc(bl + ks * 2 * kLBO, kSboB3), id, 1u);
         }
     }
 }
@@ -232,13 +234,18 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int grp = warp >> 3, gtid = tid & (kGroup - 1);
+    const int gw = warp & 7;                             // warp within the group
+    const bool issuer = lane == 0 && gw < kIssuers;      // issues the MMAs of tile (pair) gw
     const int q = warp & 3, th = (warp >> 2) & 1;   // TMEM lane quarter; tiles th, th + 2
     {
         uint4 *dst = reinterpret_cast<uint4 *>(smem + OFF_IMG);
         for (int i = tid; i < kImageBytes / 16; i += kThreads) dst[i] = image[i];
     }
     if (tid == 0) {
-        for (int i = 0; i < 4; ++i) mbar_init(&bar[i], 1);
+        mbar_init(&bar[0], 1);                  // frames: one arrival + the copy's bytes
+        mbar_init(&bar[1], 1);
+        mbar_init(&bar[2], kIssuers);           // MMAs: one commit per issuing thread
+        mbar_init(&bar[3], kIssuers);
         *abort_flag = 0;
         fence_mbar_init();
     }
@@ -289,7 +296,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     int item = 2 * static_cast<int>(blockIdx.x) + grp;
     if (gtid == 0) fetch(item);
     uint32_t fpar = 0u, mpar = 0u;
-    bool mma_pending = false;     // (gtid 0) MMAs issued, completion not yet seen
+    bool mma_pending = false;     // (issuers) MMAs issued, completion not yet seen
     uint32_t pending_par = 0u;    // the phase their completion ends
     bool failed = false;
 
@@ -360,8 +367,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (gtid == 0) {
             copy_pending = false;    // landed and read
             fetch(item + stride);    // the group's next frame, into the buffer just read
+        }
+        if (issuer) {
             tc_after();
-            issue_dft32(tmem, a_addr, smem_addr(smem + OFF_B1H), smem_addr(smem + OFF_B1L));
+            issue_dft32(tmem, a_addr, smem_addr(smem + OFF_B1H), smem_addr(smem + OFF_B1L), gw);
             issued();
         }
         wait_mma();
@@ -399,10 +408,10 @@ __global__ void __launch_bounds__(kThreads, 1)
             failed = true;
             break;
         }
-        if (gtid == 0) {
+        if (issuer) {
             mma_pending = false;
             tc_after();
-            issue_dft32(tmem, a_addr, smem_addr(smem + OFF_B1H), smem_addr(smem + OFF_B1L));
+            issue_dft32(tmem, a_addr, smem_addr(smem + OFF_B1H), smem_addr(smem + OFF_B1L), gw);
             issued();
         }
         wait_mma();
@@ -447,10 +456,10 @@ __global__ void __launch_bounds__(kThreads, 1)
             failed = true;
             break;
         }
-        if (gtid == 0) {
+        if (issuer) {
             mma_pending = false;
             tc_after();
-            issue_dft16(tmem, a_addr, smem_addr(smem + OFF_B3H), smem_addr(smem + OFF_B3L));
+            issue_dft16(tmem, a_addr, smem_addr(smem + OFF_B3H), smem_addr(smem + OFF_B3L), gw);
             issued();
         }
         wait_mma();
@@ -497,13 +506,13 @@ __global__ void __launch_bounds__(kThreads, 1)
             failed = true;
             break;
         }
-        if (gtid == 0) mma_pending = false;
+        mma_pending = false;
     }
-    if (failed && gtid == 0) {
+    if (failed) {
         // let this group's copy and MMAs in flight finish before the CTA and its
         // accumulators go (each wait bounded; the error is already recorded)
-        if (copy_pending) mbar_wait_bounded(fbar, fpar, nullptr, 0);
-        if (mma_pending) mbar_wait_bounded(mbar, pending_par, nullptr, 0);
+        if (gtid == 0 && copy_pending) mbar_wait_bounded(fbar, fpar, nullptr, 0);
+        if (issuer && mma_pending) mbar_wait_bounded(mbar, pending_par, nullptr, 0);
     }
     __syncthreads();
     if (warp == 0) {
