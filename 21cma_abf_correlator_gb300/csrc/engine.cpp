@@ -458,6 +458,10 @@ corr_status fxplan_autotune(FxPlan *p, cudaStream_t stream, corrx_tiles *out) {
     Cand best{ytile0, ct0, kt0};
     for (int fp = 0; fp < n_fplans && st == CORR_OK; ++fp) {
         if (!fengine_plan_ok(p->n_freq, fp, spectra_format(p->xmode))) continue;
+        // Plan 2 rounds the data to FP16 between its DFT stages, which raises the
+        // FP16 path's error by about half; it is chosen explicitly (corrx_set_tiles),
+        // never by the autotuner, so an autotuned engine keeps plan 0/1 numerics.
+        if (fp == 2) continue;
         if ((st = fxplan_set_tiles(p, p->n_freq, cands[0].ct, cands[0].kt, fp)) != CORR_OK) break;
         float f_ms = 0.f;
         if ((st = timed(run_f, &f_ms)) != CORR_OK) break;

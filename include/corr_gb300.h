@@ -105,7 +105,9 @@ typedef struct corrx_tiles {
     int32_t  fplan;       /* F-engine FFT plan: 0 (three passes), or at n_freq
                              16384 also 1 (four passes, twice the threads) and,
                              with FP16 spectra (CORR_X_TC_FP16) only, 2 (the
-                             DFT stages as tcgen05 matrix products)              */
+                             DFT stages as tcgen05 matrix products; faster, with
+                             about 1.5x the FP16 path's error; set explicitly,
+                             corrx_autotune keeps to plans 0 and 1)              */
     float    ms_fengine;  /* corrx_autotune: F-engine ms per max_frames pass       */
     float    ms_xengine;  /* corrx_autotune: X-engine ms per max_frames pass       */
 } corrx_tiles;
