@@ -98,9 +98,11 @@ __host__ __device__ __forceinline__ int b_of_r1(int r1) {
     const int g = r1 >> 5, l = r1 & 31;
     return 16 * ((l >> 3) + 4 * (g >> 1)) + (l & 7) + 8 * (g & 1);
 }
-// Stage-2 row of (k1, d): 32 (k1 >> 1) + 16 (k1 & 1) + d.
+// Stage-2 row of (k1, d): 32 G + 4 (k1 & 7) + (d & 3) with G = 4 (k1 >> 3) + (d >> 2),
+// so that a warp's 32 rows are eight k1 by four d: its scatter into the stage-3
+// operand then hits 32 banks (the stage-1 scatter into this one hits 16).
 __host__ __device__ __forceinline__ int r2_of(int k1, int d) {
-    return 32 * (k1 >> 1) + 16 * (k1 & 1) + d;
+    return 32 * (4 * (k1 >> 3) + (d >> 2)) + 4 * (k1 & 7) + (d & 3);
 }
 // Stage-3 row of (k1, k2a): k1 + 32 k2a for k2a < 16; the other half holds the
 // rows of Z[M-k] in the same lane of the tile four further on.
@@ -391,6 +393,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             tmem_ld16(ta + 48, v + 48);
             const float2 w = tw1[b];
             float2 wk = make_float2(1.f, 0.f);
+            // row r2_of(k1, d) = r2_of(0, d) + 128 (k1 >> 3) + 4 (k1 & 7): 16 groups per
+            // k1 >> 3, and (k1 & 7) adds 4 rows, i.e. half a group (k1 & 1) plus whole
+            // groups (k1 >> 1 & 3); d & 3 < 4 keeps the low rows inside their group
             unsigned char *const dst = sA + a_off(r2_of(0, d), c, kSboA12);
 #pragma unroll
             for (int k1 = 0; k1 < 32; ++k1) {
@@ -400,8 +405,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                     wk = cmul(wk, w);
                     y = cmul(y, wk);
                 }
-                // r2_of(k1, d) - r2_of(0, d) = 32 (k1 >> 1) + 16 (k1 & 1): whole 8-row groups
-                put_half2(dst, (4 * (k1 >> 1) + 2 * (k1 & 1)) * kSboA12, y);
+                const int drows = 128 * (k1 >> 3) + 4 * (k1 & 7);
+                put_half2(dst, (drows >> 3) * kSboA12 + (drows & 7) * 16, y);
             }
         }
         if (!end_phase()) {
@@ -423,7 +428,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int h = 0; h < 2; ++h) {
             const int t = th + 2 * h;
             const int g = 4 * t + q;
-            const int k1 = 2 * g + (lane >> 4), d = lane & 15;
+            const int k1 = 8 * (g >> 2) + (lane >> 2), d = 4 * (g & 3) + (lane & 3);
             uint32_t v[64];
             const uint32_t ta = tmem + lane_base + 64 * t;
             tmem_ld16(ta, v);

@@ -9,7 +9,8 @@ tensor-core F-engine uses. These tests check that:
   * the three DFT stages run through exactly these maps (in float64) give
     numpy's FFT, and after stage 3 the rows of Z[k] and Z[M-k] are rows p and
     512 + p (entry i against entry 15 - i), except the self-paired rows 0 and 512;
-  * the stage-1 scatter into the stage-2 operand is free of bank conflicts.
+  * the stage-2 scatter into the stage-3 operand is free of bank conflicts, and
+    the stage-1 scatter puts at most two elements in one bank.
 A planted mistake in a map must be caught.
 """
 
@@ -86,11 +87,13 @@ def check_stages(maps):
     Z, C3 = three_stage_fft(z, maps)
     ref = np.fft.fft(z)
     assert np.abs(Z - ref).max() <= 1e-9 * np.abs(ref).max()
-    # stage-2 epilogue: TMEM row -> (k1, d) = (2 (row >> 5) + ((row & 31) >> 4), row & 15)
+    # stage-2 epilogue: TMEM row -> (k1, d) = (8 (G >> 2) + (l >> 2), 4 (G & 3) + (l & 3)),
+    # G = row >> 5, l = row & 31
     for k1 in range(32):
         for d in range(16):
             row = int(maps["r2"][k1, d])
-            assert (2 * (row >> 5) + ((row & 31) >> 4), row & 15) == (k1, d)
+            g, l = row >> 5, row & 31
+            assert (8 * (g >> 2) + (l >> 2), 4 * (g & 3) + (l & 3)) == (k1, d)
     # stage-3 epilogue: thread p < 512 holds Z[p + 1024 i] in row p and Z[M - p - 1024 i]
     # in row 512 + p at entry 15 - i
     for p in range(1, 512):
@@ -114,17 +117,25 @@ def test_planted_mistake_is_caught(maps, which):
         check_stages(bad)
 
 
-def test_stage1_scatter_is_conflict_free(maps):
-    """Warp (tile t, quarter q) writes, for each k1, one 4-byte element per lane."""
-    worst = 0
+def wavefronts(words):
+    banks = {}
+    for w in words:
+        banks.setdefault(int(w) % 32, set()).add(int(w))
+    return max(len(v) for v in banks.values())
+
+
+def test_scatters_bank_conflicts(maps):
+    """Each epilogue warp writes one 4-byte element per lane into the next operand:
+    stage 2's scatter hits 32 banks, stage 1's at most two elements per bank."""
+    w1 = w2 = 0
     for warp in range(16):
-        rows1 = 128 * (warp >> 2) + 32 * (warp & 3) + np.arange(32)
-        b = maps["b"][rows1]
+        rows = 128 * (warp >> 2) + 32 * (warp & 3) + np.arange(32)
+        b = maps["b"][rows]
         c, d = b >> 4, b & 15
         for k1 in range(32):
-            words = maps["o12"][maps["r2"][k1, d], c] // 4
-            banks = {}
-            for w in words:
-                banks.setdefault(int(w) % 32, set()).add(int(w))
-            worst = max(worst, max(len(v) for v in banks.values()))
-    assert worst == 1
+            w1 = max(w1, wavefronts(maps["o12"][maps["r2"][k1, d], c] // 4))
+        inv = {int(maps["r2"][k1, dd]): (k1, dd) for k1 in range(32) for dd in range(16)}
+        kd = np.array([inv[int(r)] for r in rows])
+        for k2a in range(32):
+            w2 = max(w2, wavefronts(maps["o3"][maps["r3"][kd[:, 0], k2a], kd[:, 1]] // 4))
+    assert w2 == 1 and w1 <= 2
