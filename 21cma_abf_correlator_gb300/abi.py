@@ -254,6 +254,8 @@ SIGNATURES = {
     "corrx_set_tiles": (C.c_int, [C.c_void_p, C.POINTER(corrx_tiles)]),
     "corrx_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(corrx_tiles)]),
     "corr_autotune": (C.c_int, [C.c_void_p, C.POINTER(corrx_tiles)]),
+    "corr_get_tiles": (C.c_int, [C.c_void_p, C.POINTER(corrx_tiles)]),
+    "corr_set_tiles": (C.c_int, [C.c_void_p, C.POINTER(corrx_tiles)]),
     "corrx_run_fengine": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p,
                                     C.c_size_t, C.c_int32, C.c_int32, C.c_void_p]),
     "corrx_run_xengine": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),

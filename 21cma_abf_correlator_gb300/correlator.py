@@ -145,6 +145,17 @@ class Correlator:
         return {"ytile": t.ytile, "xct": t.xct, "xkt": t.xkt, "fplan": t.fplan,
                 "ms_fengine": t.ms_fengine, "ms_xengine": t.ms_xengine}
 
+    def tiles(self) -> dict:
+        t = abi.corrx_tiles(struct_size=C.sizeof(abi.corrx_tiles))
+        abi.check(self.lib.corr_get_tiles(self.ctx, C.byref(t)), "corr_get_tiles")
+        return {"ytile": t.ytile, "xct": t.xct, "xkt": t.xkt, "fplan": t.fplan}
+
+    def set_tiles(self, ytile: int, xct: int = 0, xkt: int = 0, fplan: int = 0) -> None:
+        """Spectra layout, tensor X tile and FFT plan (2: the tensor-core FFT, FP16 form)."""
+        t = abi.corrx_tiles(struct_size=C.sizeof(abi.corrx_tiles), ytile=ytile, xct=xct, xkt=xkt,
+                            fplan=fplan)
+        abi.check(self.lib.corr_set_tiles(self.ctx, C.byref(t)), "corr_set_tiles")
+
     def stats(self) -> abi.corr_device_stats:
         st = abi.corr_device_stats()
         abi.check(self.lib.corr_device_stats_get(self.ctx, 0, C.byref(st)), "corr_device_stats_get")

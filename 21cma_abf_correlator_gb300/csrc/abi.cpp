@@ -774,7 +774,25 @@ extern "C" corr_status corr_set_xengine(void *h, int32_t mode) {
         if (c->plan->ytile < ct) c->plan->ytile = c->plan->n_freq;
     }
     c->plan->xmode = mode;
+    // an FFT plan that cannot write this mode's spectra falls back to plan 0
+    if (!corrgb::fengine_plan_ok(c->plan->n_freq, c->plan->fplan, corrgb::spectra_format(mode)))
+        c->plan->fplan = 0;
     return CORR_OK;
+}
+
+extern "C" corr_status corr_get_tiles(void *h, corrx_tiles *out) {
+    Context *c = as_ctx(h);
+    if (c == nullptr) return fail(CORR_ERR_ARG, "ctx is NULL");
+    return corrx_get_tiles(c->plan, out);
+}
+
+extern "C" corr_status corr_set_tiles(void *h, const corrx_tiles *t) {
+    Context *c = as_ctx(h);
+    if (c == nullptr || t == nullptr) return fail(CORR_ERR_ARG, "ctx and t must be non-NULL");
+    if (c->dirty || c->pending != 0)
+        return fail(CORR_ERR_STATE,
+                    "tiles can only change while no row holds data (after create or a fetch)");
+    return corrx_set_tiles(c->plan, t);
 }
 
 extern "C" corr_status corr_autotune(void *h, corrx_tiles *out) {

@@ -116,16 +116,22 @@ corr_status corrx_get_tiles(void *eng, corrx_tiles *out);
 /* CORR_ERR_ARG for an infeasible shape; the spectra buffer's previous contents
    become meaningless (run the F-engine again). */
 corr_status corrx_set_tiles(void *eng, const corrx_tiles *t);
-/* Time every FFT plan and every feasible (ytile, xct, xkt) on this device -- F-
-   and X-engine passes of min(max_frames, 1024) synthetic frames (temporary
+/* Time FFT plans 0 and 1 and every feasible (ytile, xct, xkt) on this device --
+   F- and X-engine passes of min(max_frames, 1024) synthetic frames (temporary
    device buffers of that many frames plus one row) -- keep the fastest F-engine
-   plan and X-engine tile and report them in *out (may be NULL). Synchronises
+   plan and X-engine tile and report them in *out (may be NULL). Plan 2 (less
+   precise) is never chosen here; corrx_set_tiles selects it. Synchronises
    `stream`. */
 corr_status corrx_autotune(void *eng, void *stream, corrx_tiles *out);
 
 /* corrx_autotune for the engine inside an ABI context; allowed only while no
    row holds data, like corr_set_xengine. */
 corr_status corr_autotune(void *ctx, corrx_tiles *out);
+/* corrx_get_tiles / corrx_set_tiles for the engine inside an ABI context (set
+   only while no row holds data), e.g. to choose FFT plan 2 for the FP16 form.
+   corr_set_xengine resets an FFT plan that the new mode cannot use to plan 0. */
+corr_status corr_get_tiles(void *ctx, corrx_tiles *out);
+corr_status corr_set_tiles(void *ctx, const corrx_tiles *t);
 
 /* The two halves of corrx_accumulate, for timing and profiling each kernel on
    its own. corrx_run_fengine transforms `frames` (<= max_frames) frames into the

@@ -16,7 +16,8 @@ ALL_VALID, HOST_ZEROED, MASK_MARKED = "all_valid", "host_zeroed", "mask_marked"
 def drive_rows(pkg, x: np.ndarray, n_cum: int, frames_per_slot: int, mode: str = ALL_VALID,
                missing: np.ndarray | None = None, present: np.ndarray | None = None,
                xmode: int = 0, block_slots: int = 3, chunk_frames: int | None = None,
-               rows_per_fetch: int | None = None, autotune: bool = False):
+               rows_per_fetch: int | None = None, autotune: bool = False,
+               fplan: int | None = None):
     """x: int8 [rows, n_station, n_cum, 2*n_freq] -> complex64 [rows, n_baseline, n_freq].
 
     missing: bool [rows, n_cum] frames handled per `mode` (golden.c's three
@@ -32,6 +33,9 @@ def drive_rows(pkg, x: np.ndarray, n_cum: int, frames_per_slot: int, mode: str =
             c.set_xengine(xmode)
         if autotune:
             c.autotune()
+        if fplan is not None:
+            t = c.tiles()
+            c.set_tiles(t["ytile"], t["xct"], t["xkt"], fplan)
         views = [c.staging(g) for g in range(n)]
         submits = 0
         for r in range(rows):

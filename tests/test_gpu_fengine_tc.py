@@ -117,3 +117,26 @@ def test_autotune_at_16384_keeps_the_cuda_core_plans(pkg, cuda, oracle, xmode):
         eng.close()
     ref = oracle.correlate(x)
     assert oracle.rel_rms(got, ref) <= 2.5e-3 / np.sqrt(frames)
+
+
+def test_plan2_through_the_abi(pkg, cuda, oracle):
+    """corr_set_tiles chooses plan 2 for an ABI context; rows match the oracle."""
+    from abi_driver import drive_rows
+    rows, n, n_cum = 2, 4, 40
+    rng = np.random.default_rng(23)
+    x = np.clip(np.rint(24 * rng.standard_normal((rows, n, n_cum, 2 * NF))), -128, 127).astype(
+        np.int8)
+    got = drive_rows(pkg, x, n_cum, 16, xmode=pkg.abi.CORR_X_TC_FP16, fplan=2)
+    ref = oracle.correlate_rows(x, n_cum)
+    assert oracle.rel_rms(got, ref) <= 2.5e-3 / np.sqrt(n_cum)
+
+
+def test_set_xengine_resets_a_plan_the_mode_cannot_use(pkg, cuda):
+    cfg = pkg.make_config(2, NF, 16, 16, 3, 1)
+    with pkg.Correlator(cfg) as c:
+        c.set_xengine(pkg.abi.CORR_X_TC_FP16)
+        t = c.tiles()
+        c.set_tiles(t["ytile"], t["xct"], t["xkt"], 2)
+        assert c.tiles()["fplan"] == 2
+        c.set_xengine(pkg.abi.CORR_X_TC_FP16_SPLIT)
+        assert c.tiles()["fplan"] == 0
