@@ -10,7 +10,8 @@ delays from rows; synth.py generates the seeded workloads.
 
 from . import abi
 from .abi import CorrError
-from .correlator import Correlator, make_config
+from .correlator import Correlator, make_config, plan_query, set_device_map
 from .engine import FxEngine
 
-__all__ = ["abi", "CorrError", "Correlator", "make_config", "FxEngine"]
+__all__ = ["abi", "CorrError", "Correlator", "make_config", "plan_query", "set_device_map",
+           "FxEngine"]

@@ -23,6 +23,9 @@ CORR_X_PLAIN_FP32 = 0
 CORR_X_TC_FP16 = 1
 CORR_X_TC_FP16_SPLIT = 2
 
+CORRX_ACC_FP32 = 0
+CORRX_ACC_FP64 = 1
+
 STATUS_NAMES = {
     0: "CORR_OK",
     1: "CORR_ERR_ARG",
@@ -249,6 +252,13 @@ SIGNATURES = {
     "corrx_accumulate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_size_t, C.c_void_p,
                                    C.c_size_t, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "corrx_scale": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "corrx_set_accumulator": (C.c_int, [C.c_void_p, C.c_int32]),
+    "corrx_dump": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
+    "corrx_set_device_map": (C.c_int, [C.POINTER(C.c_int32), C.c_int32]),
+    "corrx_plan_query": (C.c_int, [C.POINTER(corr_config), C.c_int32,
+                                   C.POINTER(corr_device_plan), C.POINTER(C.c_int32), C.c_int32,
+                                   C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int32),
+                                   C.c_int32]),
     "corrx_check": (C.c_int, [C.c_void_p]),
     "corrx_get_tiles": (C.c_int, [C.c_void_p, C.POINTER(corrx_tiles)]),
     "corrx_set_tiles": (C.c_int, [C.c_void_p, C.POINTER(corrx_tiles)]),

@@ -29,7 +29,10 @@ class StagingView:
 
 def make_config(n_station: int, n_freq: int, frames_per_slot: int, chunk_frames: int,
                 block_slots: int = 3, rows_per_fetch: int = 1, device_id: int = 0,
-                split_mode: int = abi.CORR_SPLIT_BASELINE_RANGE) -> abi.corr_config:
+                split_mode: int = abi.CORR_SPLIT_BASELINE_RANGE,
+                devices: list[int] | None = None) -> abi.corr_config:
+    """A corr_config; `devices` (up to CORR_MAX_DEVICES ordinals) spreads the run
+    over several devices with `split_mode`, else device_id alone is used."""
     cfg = abi.corr_config()
     cfg.abi_version = abi.CORR_ABI_VERSION
     cfg.struct_size = C.sizeof(abi.corr_config)
@@ -41,8 +44,39 @@ def make_config(n_station: int, n_freq: int, frames_per_slot: int, chunk_frames:
     cfg.block_slots = block_slots
     cfg.rows_per_fetch = rows_per_fetch
     cfg.n_devices = 0
+    if devices:
+        cfg.n_devices = len(devices)
+        for i, d in enumerate(devices):
+            cfg.devices[i] = d
     cfg.split_mode = split_mode
     return cfg
+
+
+def plan_query(cfg: abi.corr_config, device_index: int) -> dict:
+    """The placement corr_create makes for `cfg` on one device (corrx_plan_query),
+    computed on the host without a GPU."""
+    lib = abi.load()
+    plan = abi.corr_device_plan()
+    nb = lib.corr_n_baseline(cfg.n_station)
+    st = (C.c_int32 * cfg.n_station)()
+    bl = (C.c_int32 * nb)()
+    lo = (C.c_int32 * nb)()
+    abi.check(lib.corrx_plan_query(C.byref(cfg), device_index, C.byref(plan), st, cfg.n_station,
+                                   bl, nb, lo, nb), "corrx_plan_query")
+    return {"device_id": plan.device_id, "n_station_resident": plan.n_station_resident,
+            "first_baseline": plan.first_baseline, "n_baseline": plan.n_baseline,
+            "contiguous": bool(plan.contiguous),
+            "stations": list(st[:plan.n_station_resident]),
+            "baselines": list(bl[:plan.n_baseline]), "local": list(lo[:plan.n_baseline])}
+
+
+def set_device_map(physical: list[int] | None) -> None:
+    """Run configured device i of later contexts on CUDA device physical[i]
+    (corrx_set_device_map); None or [] restores the identity."""
+    lib = abi.load()
+    phys = physical or []
+    arr = (C.c_int32 * max(1, len(phys)))(*phys)
+    abi.check(lib.corrx_set_device_map(arr, len(phys)), "corrx_set_device_map")
 
 
 class Correlator:
@@ -156,10 +190,32 @@ class Correlator:
                             fplan=fplan)
         abi.check(self.lib.corr_set_tiles(self.ctx, C.byref(t)), "corr_set_tiles")
 
-    def stats(self) -> abi.corr_device_stats:
+    def stats(self, device_index: int = 0) -> abi.corr_device_stats:
         st = abi.corr_device_stats()
-        abi.check(self.lib.corr_device_stats_get(self.ctx, 0, C.byref(st)), "corr_device_stats_get")
+        abi.check(self.lib.corr_device_stats_get(self.ctx, device_index, C.byref(st)),
+                  "corr_device_stats_get")
         return st
+
+    def n_devices(self) -> int:
+        return self.lib.corr_n_devices(self.ctx)
+
+    def device_plan(self, device_index: int) -> dict:
+        """What device `device_index` holds and owns (corr_device_plan_get,
+        corr_device_stations, corr_device_baselines)."""
+        plan = abi.corr_device_plan()
+        abi.check(self.lib.corr_device_plan_get(self.ctx, device_index, C.byref(plan)),
+                  "corr_device_plan_get")
+        st = (C.c_int32 * max(1, plan.n_station_resident))()
+        bl = (C.c_int32 * max(1, plan.n_baseline))()
+        abi.check(self.lib.corr_device_stations(self.ctx, device_index, st,
+                                                plan.n_station_resident), "corr_device_stations")
+        abi.check(self.lib.corr_device_baselines(self.ctx, device_index, bl, plan.n_baseline),
+                  "corr_device_baselines")
+        return {"device_id": plan.device_id, "n_station_resident": plan.n_station_resident,
+                "first_baseline": plan.first_baseline, "n_baseline": plan.n_baseline,
+                "contiguous": bool(plan.contiguous),
+                "stations": list(st[:plan.n_station_resident]),
+                "baselines": list(bl[:plan.n_baseline])}
 
     @staticmethod
     def baseline_pairs(n_station: int) -> list[tuple[int, int]]:

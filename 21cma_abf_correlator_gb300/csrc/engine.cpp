@@ -41,8 +41,18 @@ corr_status failf(corr_status st, const char *fmt, ...) {
 
 corr_status cuda_check(cudaError_t e, const char *what) {
     if (e == cudaSuccess) return CORR_OK;
+    cudaGetLastError();   // a failed call must not surface again at the next launch check
     return fail(CORR_ERR_CUDA,
                 std::string(what) + ": " + cudaGetErrorName(e) + ": " + cudaGetErrorString(e));
+}
+
+corr_status PerDevice::fail_current() {
+    return fail(CORR_ERR_CUDA, "cudaGetDevice failed: no current device");
+}
+
+corr_status PerDevice::fail_ordinal(int dev) {
+    return failf(CORR_ERR_ARG, "device ordinal %d: at most %d devices are supported", dev,
+                 kMaxDeviceOrdinals);
 }
 
 static bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
@@ -134,7 +144,7 @@ void fxplan_destroy(FxPlan *p) {
 corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_stride,
                               size_t frame_stride, const uint8_t *mask,
                               size_t mask_station_stride, int mask_bit0, int frames,
-                              float2 *acc, cudaStream_t stream, const uint32_t *pmask,
+                              void *acc, cudaStream_t stream, const uint32_t *pmask,
                               size_t pmask_station_stride, int pmask_frame0) {
     if (frames < 0) return fail(CORR_ERR_ARG, "frames must be >= 0");
     const size_t frame_bytes = 2u * static_cast<size_t>(p->n_freq);
@@ -176,6 +186,7 @@ corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_s
         xa.n_freq = p->n_freq;
         xa.frames = ft;
         xa.acc = acc;
+        xa.acc64 = p->acc64;
         xa.err = p->d_err;
         if (p->xmode == CORR_X_PLAIN_FP32)
             st = xengine_plain_launch(xa, p->num_sms, stream);
@@ -248,8 +259,8 @@ extern "C" corr_status corrx_accumulate(void *eng, const int8_t *d_samples,
     corr_status st = cuda_check(cudaSetDevice(p->device), "cudaSetDevice");
     if (st != CORR_OK) return st;
     return fxplan_accumulate(p, d_samples, station_stride, frame_stride, d_mask,
-                             mask_station_stride, mask_bit0, frames,
-                             static_cast<float2 *>(d_acc), static_cast<cudaStream_t>(stream));
+                             mask_station_stride, mask_bit0, frames, d_acc,
+                             static_cast<cudaStream_t>(stream));
 }
 
 extern "C" corr_status corrx_accumulate_packets(void *eng, const int8_t *d_samples,
@@ -272,9 +283,9 @@ extern "C" corr_status corrx_accumulate_packets(void *eng, const int8_t *d_sampl
     corr_status st = cuda_check(cudaSetDevice(p->device), "cudaSetDevice");
     if (st != CORR_OK) return st;
     return fxplan_accumulate(p, d_samples, station_stride, frame_stride, d_mask,
-                             mask_station_stride, mask_bit0, frames,
-                             static_cast<float2 *>(d_acc), static_cast<cudaStream_t>(stream),
-                             d_pmask, pmask_station_stride, pmask_frame0);
+                             mask_station_stride, mask_bit0, frames, d_acc,
+                             static_cast<cudaStream_t>(stream), d_pmask, pmask_station_stride,
+                             pmask_frame0);
 }
 
 extern "C" corr_status corrx_scale(void *eng, void *d_acc, uint64_t frames, void *stream) {
@@ -283,9 +294,45 @@ extern "C" corr_status corrx_scale(void *eng, void *d_acc, uint64_t frames, void
     if (frames == 0) return fail(CORR_ERR_ARG, "frames must be > 0");
     corr_status st = cuda_check(cudaSetDevice(p->device), "cudaSetDevice");
     if (st != CORR_OK) return st;
-    return scale_launch(static_cast<float2 *>(d_acc),
-                        static_cast<size_t>(p->n_baseline) * p->n_freq,
-                        1.0f / static_cast<float>(frames), static_cast<cudaStream_t>(stream));
+    const size_t n = static_cast<size_t>(p->n_baseline) * p->n_freq;
+    if (p->acc64)
+        return scale64_launch(static_cast<double2 *>(d_acc), n,
+                              1.0 / static_cast<double>(frames), static_cast<cudaStream_t>(stream));
+    return scale_launch(static_cast<float2 *>(d_acc), n, 1.0f / static_cast<float>(frames),
+                        static_cast<cudaStream_t>(stream));
+}
+
+extern "C" corr_status corrx_set_accumulator(void *eng, int32_t precision) {
+    FxPlan *p = static_cast<FxPlan *>(eng);
+    if (p == nullptr) return fail(CORR_ERR_ARG, "eng is NULL");
+    if (precision != CORRX_ACC_FP32 && precision != CORRX_ACC_FP64)
+        return failf(CORR_ERR_ARG, "unknown accumulator precision %d", precision);
+    p->acc64 = precision == CORRX_ACC_FP64 ? 1 : 0;
+    return CORR_OK;
+}
+
+extern "C" corr_status corrx_dump(void *eng, const void *d_acc, uint64_t frames, void *d_out,
+                                  void *stream) {
+    FxPlan *p = static_cast<FxPlan *>(eng);
+    if (p == nullptr) return fail(CORR_ERR_ARG, "eng is NULL");
+    if (d_acc == nullptr || d_out == nullptr) return fail(CORR_ERR_ARG, "d_acc and d_out must be non-NULL");
+    if (frames == 0) return fail(CORR_ERR_ARG, "frames must be > 0");
+    if ((reinterpret_cast<uintptr_t>(d_acc) | reinterpret_cast<uintptr_t>(d_out)) % 16 != 0)
+        return fail(CORR_ERR_ARG, "d_acc and d_out must be 16-byte aligned");
+    corr_status st = cuda_check(cudaSetDevice(p->device), "cudaSetDevice");
+    if (st != CORR_OK) return st;
+    const size_t n = static_cast<size_t>(p->n_baseline) * p->n_freq;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (p->acc64)
+        return dump64_launch(static_cast<float2 *>(d_out), n, static_cast<const double2 *>(d_acc),
+                             n, nullptr, nullptr, p->n_baseline, p->n_freq, 1,
+                             1.0 / static_cast<double>(frames), s);
+    if (d_out != d_acc &&
+        (st = cuda_check(cudaMemcpyAsync(d_out, d_acc, n * sizeof(float2),
+                                         cudaMemcpyDeviceToDevice, s),
+                         "cudaMemcpyAsync(dump)")) != CORR_OK)
+        return st;
+    return scale_launch(static_cast<float2 *>(d_out), n, 1.0f / static_cast<float>(frames), s);
 }
 
 extern "C" corr_status corrx_run_fengine(void *eng, const int8_t *d_samples,
@@ -336,7 +383,8 @@ extern "C" corr_status corrx_run_xengine(void *eng, int32_t frames, void *d_acc,
     xa.n_station = p->n_station;
     xa.n_freq = p->n_freq;
     xa.frames = frames;
-    xa.acc = static_cast<float2 *>(d_acc);
+    xa.acc = d_acc;
+    xa.acc64 = p->acc64;
     xa.err = p->d_err;
     if (p->xmode == CORR_X_PLAIN_FP32)
         return xengine_plain_launch(xa, p->num_sms, static_cast<cudaStream_t>(stream));
@@ -403,9 +451,10 @@ corr_status fxplan_autotune(FxPlan *p, cudaStream_t stream, corrx_tiles *out) {
     const int frames = std::min(p->max_frames, 1024);
     const int L = 2 * p->n_freq;
     const size_t x_bytes = static_cast<size_t>(p->n_station) * frames * L;
-    const size_t acc_bytes = static_cast<size_t>(p->n_baseline) * p->n_freq * sizeof(float2);
+    // room for a complex128 row, whichever accumulator the engine uses
+    const size_t acc_bytes = static_cast<size_t>(p->n_baseline) * p->n_freq * sizeof(double2);
     int8_t *d_x = nullptr;
-    float2 *d_acc = nullptr;
+    void *d_acc = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     const int ytile0 = p->ytile, ct0 = p->xct, kt0 = p->xkt;
     auto cleanup = [&] {
@@ -576,6 +625,7 @@ struct FxBatch {
     cudaGraphExec_t exec = nullptr;
     std::vector<cudaEvent_t> ev_fork;
     unsigned long long *d_stamps = nullptr;   // [block][start, row in host memory], ns
+    double2 *d_acc64 = nullptr;   // complex128 accumulator of the block in flight (FP64 engines)
     cudaStream_t cap = nullptr, side = nullptr;
     cudaStream_t last_launch = nullptr;
 };
@@ -587,6 +637,7 @@ void batch_free(FxBatch *b) {
     for (cudaEvent_t e : b->ev_fork)
         if (e) cudaEventDestroy(e);
     if (b->d_stamps) cudaFree(b->d_stamps);
+    if (b->d_acc64) cudaFree(b->d_acc64);
     if (b->cap) cudaStreamDestroy(b->cap);
     if (b->side) cudaStreamDestroy(b->side);
     delete b;
@@ -615,9 +666,11 @@ corr_status batch_create(const std::vector<FxPlan *> &plans, const int32_t *bloc
         if (q == nullptr) return fail(CORR_ERR_ARG, "an engine is NULL");
     FxPlan *p = plans[0];
     for (FxPlan *q : plans)
-        if (q->device != p->device || q->n_station != p->n_station || q->n_freq != p->n_freq)
+        if (q->device != p->device || q->n_station != p->n_station || q->n_freq != p->n_freq ||
+            q->acc64 != p->acc64)
             return fail(CORR_ERR_ARG,
-                        "the engines of one batch must share device, n_station and n_freq");
+                        "the engines of one batch must share device, n_station, n_freq and "
+                        "accumulator precision");
     if (d_samples == nullptr || d_rows == nullptr || block_first == nullptr ||
         block_frames == nullptr)
         return fail(CORR_ERR_ARG, "d_samples, d_rows and the block arrays must be non-NULL");
@@ -659,6 +712,13 @@ corr_status batch_create(const std::vector<FxPlan *> &plans, const int32_t *bloc
     for (int i = 0; i <= n_blocks && st == CORR_OK; ++i)
         st = cuda_check(cudaEventCreateWithFlags(&b->ev_fork[i], cudaEventDisableTiming),
                         "cudaEventCreate");
+    // FP64 engines accumulate each block in one complex128 row, reused block
+    // after block (the blocks run in order on the capture stream), and dump it
+    // scaled into the block's complex64 row.
+    if (st == CORR_OK && p->acc64)
+        st = cuda_check(cudaMalloc(&b->d_acc64, row_elems * sizeof(double2)),
+                        "cudaMalloc(FP64 row)");
+    void *acc_of_block = p->acc64 ? static_cast<void *>(b->d_acc64) : static_cast<void *>(rows);
     if (st != CORR_OK) {
         batch_free(b);
         return st;
@@ -671,7 +731,7 @@ corr_status batch_create(const std::vector<FxPlan *> &plans, const int32_t *bloc
         if (used)
             st = fxplan_accumulate(plans[e], d_samples, station_stride, frame_stride, d_mask,
                                    mask_station_stride, static_cast<int>(block_first[0]), 1,
-                                   rows, b->cap, d_pmask, pmask_station_stride,
+                                   acc_of_block, b->cap, d_pmask, pmask_station_stride,
                                    static_cast<int>(block_first[0]));
     }
     if (st == CORR_OK) st = cuda_check(cudaStreamSynchronize(b->cap), "warm-up");
@@ -685,19 +745,25 @@ corr_status batch_create(const std::vector<FxPlan *> &plans, const int32_t *bloc
     for (int i = 0; i < n_blocks && st == CORR_OK; ++i) {
         float2 *row = rows + static_cast<size_t>(i) * row_elems;
         const int first = static_cast<int>(block_first[i]);
+        const size_t acc_bytes = row_elems * (p->acc64 ? sizeof(double2) : sizeof(float2));
+        void *acc = p->acc64 ? static_cast<void *>(b->d_acc64) : static_cast<void *>(row);
         if ((st = stamp_launch(b->d_stamps + 2 * i, b->cap)) != CORR_OK) break;
-        if ((st = cuda_check(cudaMemsetAsync(row, 0, row_elems * sizeof(float2), b->cap),
+        if ((st = cuda_check(cudaMemsetAsync(acc, 0, acc_bytes, b->cap),
                              "cudaMemsetAsync(row)")) != CORR_OK)
             break;
         if ((st = fxplan_accumulate(plan_of(i),
                                     d_samples + static_cast<size_t>(first) * frame_stride,
                                     station_stride, frame_stride, d_mask, mask_station_stride,
-                                    first, block_frames[i], row, b->cap, d_pmask,
+                                    first, block_frames[i], acc, b->cap, d_pmask,
                                     pmask_station_stride, first)) != CORR_OK)
             break;
-        if ((st = scale_launch(row, row_elems, 1.0f / static_cast<float>(block_frames[i]),
-                               b->cap)) != CORR_OK)
-            break;
+        if (p->acc64)
+            st = dump64_launch(row, row_elems, b->d_acc64, row_elems, nullptr, nullptr,
+                               p->n_baseline, p->n_freq, 1,
+                               1.0 / static_cast<double>(block_frames[i]), b->cap);
+        else
+            st = scale_launch(row, row_elems, 1.0f / static_cast<float>(block_frames[i]), b->cap);
+        if (st != CORR_OK) break;
         // dump on the side stream; the next block's kernels do not wait for it
         if ((st = cuda_check(cudaEventRecord(b->ev_fork[i], b->cap), "cudaEventRecord")) != CORR_OK ||
             (st = cuda_check(cudaStreamWaitEvent(b->side, b->ev_fork[i], 0), "cudaStreamWaitEvent")) !=

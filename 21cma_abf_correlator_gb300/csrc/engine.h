@@ -12,8 +12,11 @@
 #include <cstddef>
 #include <cstdint>
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <mutex>
 #include <string>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -27,6 +30,38 @@ std::string &last_error();
 corr_status fail(corr_status st, const std::string &msg);
 corr_status failf(corr_status st, const char *fmt, ...);
 corr_status cuda_check(cudaError_t e, const char *what);
+
+/// Device ordinals a process-wide per-device record can hold.
+constexpr int kMaxDeviceOrdinals = 64;
+
+/// A one-time set-up that must happen once on every device a kernel runs on
+/// (cudaFuncSetAttribute and occupancy queries are per-device), safe against
+/// concurrent first calls from several threads. run() executes `fn` with the
+/// current device unless it already succeeded there; a failure is not recorded,
+/// so the next call tries again.
+class PerDevice {
+public:
+    template <class F> corr_status run(F &&fn) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) {
+            cudaGetLastError();
+            return fail_current();
+        }
+        if (dev < 0 || dev >= kMaxDeviceOrdinals) return fail_ordinal(dev);
+        if (done_[dev].load(std::memory_order_acquire)) return CORR_OK;
+        std::lock_guard<std::mutex> lock(mu_);
+        if (done_[dev].load(std::memory_order_relaxed)) return CORR_OK;
+        const corr_status st = fn(dev);
+        if (st == CORR_OK) done_[dev].store(true, std::memory_order_release);
+        return st;
+    }
+
+private:
+    static corr_status fail_current();
+    static corr_status fail_ordinal(int dev);
+    std::mutex mu_;
+    std::atomic<bool> done_[kMaxDeviceOrdinals] = {};
+};
 
 /// Watchdog codes a kernel writes into FxPlan::d_err when a bounded wait ran out.
 enum : int {
@@ -113,6 +148,11 @@ struct FengineArgs {
 };
 
 /// Arguments of one X-engine launch over `frames` frames of spectra.
+///
+/// The launch sums its frames in FP32 (registers or tensor memory) and adds that
+/// partial sum into the row once, in its epilogue: into complex64 values
+/// (acc64 = 0) or into complex128 values (acc64 = 1), the cross-launch
+/// integration accumulator that keeps long rows at the precision of one launch.
 struct XengineArgs {
     const float2 *y;            // as FengineArgs::y
     int y_frames;               // frames the spectra buffer holds (>= frames)
@@ -121,11 +161,19 @@ struct XengineArgs {
     int n_station;
     int n_freq;
     int frames;
-    float2 *acc;                // acc[b*n_freq + c] +=
+    void *acc;                  // acc[b*n_freq + c] += (float2, or double2 if acc64)
+    int acc64;
     int *err;
 };
 
 // fengine.cu
+/// Entries of the four twiddle tables for n_freq (pass_lo, pass_hi, post_lo, post_hi).
+constexpr int twiddle_entries(int n_freq) { return 128 + 2 * (n_freq / 64); }
+/// The four tables for n_freq, concatenated in that order (host, double
+/// precision rounded once to float).
+void fengine_twiddles_host(int n_freq, std::vector<float2> *all);
+/// Point `tw` at the four tables stored concatenated from `base` (device memory).
+void twiddle_views(float2 *base, int n_freq, TwiddleTables *tw);
 corr_status fengine_prepare(int n_freq, TwiddleTables *tw);
 /// How many FFT radix plans the F-engine has for n_freq (plan 0 always exists).
 int fengine_plans(int n_freq);
@@ -142,6 +190,16 @@ corr_status fengine_launch(int n_freq, const TwiddleTables &tw, const FengineArg
 // xengine.cu
 corr_status xengine_plain_launch(const XengineArgs &a, int num_sms, cudaStream_t stream);
 corr_status scale_launch(float2 *acc, size_t n, float s, cudaStream_t stream);
+/// acc[i] *= s in double precision over n complex128 values.
+corr_status scale64_launch(double2 *acc, size_t n, double s, cudaStream_t stream);
+/// dst[i] += src[i] over n complex128 values.
+corr_status add64_launch(double2 *dst, const double2 *src, size_t n, cudaStream_t stream);
+/// Complex128 rows to complex64: for r < rows, i < n_map, c < n_freq,
+///   out[r*out_row + gmap[i]*n_freq + c] = (float2)(src[r*src_row + lmap[i]*n_freq + c] * s)
+/// (gmap/lmap NULL: the identity over n_map baselines). n_freq is even.
+corr_status dump64_launch(float2 *out, size_t out_row, const double2 *src, size_t src_row,
+                          const int32_t *gmap, const int32_t *lmap, int n_map, int n_freq,
+                          int rows, double s, cudaStream_t stream);
 corr_status watchdog_selftest_launch(int *err, long long budget_cycles, cudaStream_t stream);
 corr_status stamp_launch(unsigned long long *slot, cudaStream_t stream);
 /// Deterministic pseudo-random int8 samples (roughly Gaussian, sigma ~ 24) for
@@ -170,6 +228,7 @@ struct FxPlan {
     int xkt = 0;          // tensor X-engine: frames per stage
     int fplan = 0;        // F-engine FFT radix plan
     int xmode = CORR_X_PLAIN_FP32;
+    int acc64 = 0;        // rows are complex128 (CORRX_ACC_FP64) instead of complex64
     int num_sms = 0;
     float2 *d_y = nullptr;
     int *d_err = nullptr;
@@ -186,7 +245,7 @@ corr_status fxplan_autotune(FxPlan *p, cudaStream_t stream, corrx_tiles *out);
 corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_stride,
                               size_t frame_stride, const uint8_t *mask,
                               size_t mask_station_stride, int mask_bit0, int frames,
-                              float2 *acc, cudaStream_t stream,
+                              void *acc, cudaStream_t stream,
                               const uint32_t *pmask = nullptr, size_t pmask_station_stride = 0,
                               int pmask_frame0 = 0);
 

@@ -443,27 +443,31 @@ template <int LOGM, int PLAN, int FMT, bool CONTIG>
 corr_status launch_one(const FengineArgs &a, const TwiddleTables &tw, int num_sms,
                        cudaStream_t stream) {
     using C = FeCfg<LOGM, PLAN>;
-    static bool configured = false;
-    static int per_sm = 1;
-    if (!configured) {
-        corr_status st = cuda_check(
+    // Shared-memory limit and residency are per device: set up once on each.
+    static PerDevice setup;
+    static int per_sm[kMaxDeviceOrdinals];
+    corr_status st = setup.run([](int dev) {
+        corr_status s2 = cuda_check(
             cudaFuncSetAttribute(fengine_kernel<LOGM, PLAN, FMT, CONTIG>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM),
             "cudaFuncSetAttribute(fengine)");
-        if (st != CORR_OK) return st;
+        if (s2 != CORR_OK) return s2;
         int blocks = 0;
-        st = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        s2 = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                             &blocks, fengine_kernel<LOGM, PLAN, FMT, CONTIG>, C::T, C::SMEM),
                         "cudaOccupancyMaxActiveBlocksPerMultiprocessor(fengine)");
-        if (st != CORR_OK) return st;
+        if (s2 != CORR_OK) return s2;
         if (blocks < 1)
             return fail(CORR_ERR_INTERNAL, "F-engine kernel cannot be resident on an SM");
-        per_sm = blocks;
-        configured = true;
-    }
+        per_sm[dev] = blocks;
+        return CORR_OK;
+    });
+    if (st != CORR_OK) return st;
+    int dev = 0;
+    cudaGetDevice(&dev);
     const int items = a.frames * a.n_station;
     if (items <= 0) return CORR_OK;
-    int grid = num_sms * per_sm;
+    int grid = num_sms * per_sm[dev];
     if (grid > items) grid = items;
     TwPtrs p{tw.pass_lo, tw.pass_hi, tw.post_lo, tw.post_hi};
     fengine_kernel<LOGM, PLAN, FMT, CONTIG><<<grid, C::T, C::SMEM, stream>>>(a, p);
@@ -511,47 +515,43 @@ bool fengine_plan_ok(int n_freq, int fplan, int y_fmt) {
     return fplan != 2 || y_fmt == kSpectraF16;   // the tensor-core plan writes FP16 only
 }
 
-corr_status fengine_prepare(int n_freq, TwiddleTables *tw) {
+void fengine_twiddles_host(int n_freq, std::vector<float2> *all) {
     const int M = n_freq;
     const double pi = 3.14159265358979323846;
-    std::vector<float2> h_plo(64), h_phi(static_cast<size_t>(M / 64)), h_qlo(64),
-        h_qhi(static_cast<size_t>(M / 64));
-    for (int u = 0; u < 64; ++u) {
-        const double a = -2.0 * pi * u / M;
-        h_plo[u] = make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
-        const double b = -pi * u / M;
-        h_qlo[u] = make_float2(static_cast<float>(std::cos(b)), static_cast<float>(std::sin(b)));
-    }
-    for (int u = 0; u < M / 64; ++u) {
-        const double a = -2.0 * pi * 64.0 * u / M;
-        h_phi[u] = make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
-    }
-    for (int u = 0; u < M / 64; ++u) {
-        const double b = -pi * 64.0 * u / M;
-        h_qhi[u] = make_float2(static_cast<float>(std::cos(b)), static_cast<float>(std::sin(b)));
-    }
-    tw->n_pass_hi = M / 64;
-    tw->n_post_hi = M / 64;
-    const size_t n_all = 64 + h_phi.size() + 64 + h_qhi.size();
+    auto cis = [](double a) {
+        return make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
+    };
+    all->clear();
+    all->reserve(static_cast<size_t>(twiddle_entries(n_freq)));
+    for (int u = 0; u < 64; ++u) all->push_back(cis(-2.0 * pi * u / M));            // pass_lo
+    for (int u = 0; u < M / 64; ++u) all->push_back(cis(-2.0 * pi * 64.0 * u / M)); // pass_hi
+    for (int u = 0; u < 64; ++u) all->push_back(cis(-pi * u / M));                  // post_lo
+    for (int u = 0; u < M / 64; ++u) all->push_back(cis(-pi * 64.0 * u / M));       // post_hi
+}
+
+void twiddle_views(float2 *base, int n_freq, TwiddleTables *tw) {
+    tw->n_pass_hi = n_freq / 64;
+    tw->n_post_hi = n_freq / 64;
+    tw->pass_lo = base;
+    tw->pass_hi = base + 64;
+    tw->post_lo = tw->pass_hi + tw->n_pass_hi;
+    tw->post_hi = tw->post_lo + 64;
+}
+
+corr_status fengine_prepare(int n_freq, TwiddleTables *tw) {
+    std::vector<float2> all;
+    fengine_twiddles_host(n_freq, &all);
+    const size_t n_all = all.size();
     float2 *d = nullptr;
     corr_status st = cuda_check(cudaMalloc(&d, n_all * sizeof(float2)), "cudaMalloc(twiddles)");
     if (st != CORR_OK) return st;
-    std::vector<float2> all;
-    all.reserve(n_all);
-    all.insert(all.end(), h_plo.begin(), h_plo.end());
-    all.insert(all.end(), h_phi.begin(), h_phi.end());
-    all.insert(all.end(), h_qlo.begin(), h_qlo.end());
-    all.insert(all.end(), h_qhi.begin(), h_qhi.end());
     st = cuda_check(cudaMemcpy(d, all.data(), n_all * sizeof(float2), cudaMemcpyHostToDevice),
                     "cudaMemcpy(twiddles)");
     if (st != CORR_OK) {
         cudaFree(d);
         return st;
     }
-    tw->pass_lo = d;
-    tw->pass_hi = d + 64;
-    tw->post_lo = tw->pass_hi + h_phi.size();
-    tw->post_hi = tw->post_lo + 64;
+    twiddle_views(d, n_freq, tw);
     if (n_freq == 16384 && (st = fengine_tc_prepare(&tw->tc_image)) != CORR_OK) {
         fengine_release(tw);
         return st;

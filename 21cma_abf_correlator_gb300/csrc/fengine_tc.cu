@@ -531,15 +531,13 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 template <bool CONTIG>
 corr_status launch(const FengineArgs &a, const void *image, int num_sms, cudaStream_t stream) {
-    static bool configured = false;
-    if (!configured) {
-        corr_status st = cuda_check(
-            cudaFuncSetAttribute(fengine_tc_kernel<CONTIG>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem),
-            "cudaFuncSetAttribute(fengine_tc)");
-        if (st != CORR_OK) return st;
-        configured = true;
-    }
+    static PerDevice setup;   // the shared-memory limit is a per-device setting
+    corr_status st = setup.run([](int) {
+        return cuda_check(cudaFuncSetAttribute(fengine_tc_kernel<CONTIG>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem),
+                          "cudaFuncSetAttribute(fengine_tc)");
+    });
+    if (st != CORR_OK) return st;
     const int items = a.frames * a.n_station;
     if (items <= 0) return CORR_OK;
     const int pairs = (items + 1) / 2;   // each CTA carries two items at a time

@@ -1,34 +1,37 @@
 // noalloc.cu -- corrx_accumulate for callers that cannot allocate device memory.
 //
-// Some hosts of this library may not call cudaMalloc at all: an application that
-// owns all device memory through its own pool and forbids allocation by plugins,
-// code running inside stream capture or a real-time loop where an allocation
-// (and the device-wide synchronisation it can imply) is not allowed, or a host
-// that links the library into a process whose memory budget is fixed up front.
-// corrx_accumulate_noalloc serves them: it runs the same F-engine and X-engine
-// kernels as corrx_accumulate, but the spectra between the two live in a
-// file-scope device array of fixed size instead of a buffer allocated by
-// corrx_create, and the twiddle tables are computed into a second fixed array.
+// Some hosts of this library may not call cudaMalloc at all: an application
+// that owns all device memory through its own pool and does not let plugins
+// allocate, a real-time loop in which an allocation (and the device-wide
+// synchronisation it can imply) would break the loop's deadline, or a process
+// whose device-memory budget is fixed up front. corrx_accumulate_noalloc serves
+// them: it runs the same F-engine and X-engine kernels as corrx_accumulate, but
+// the spectra between the two live in a file-scope device array of fixed size
+// instead of a buffer allocated by corrx_create, and the twiddle tables of every
+// transform length live in a second fixed array.
 //
 // Properties a caller must know:
-//   * scratch: kNoAllocScratchBytes (64 MiB) of spectra plus a few KB of twiddle
+//   * scratch: kNoAllocScratchBytes (64 MiB) of spectra plus 14 KB of twiddle
 //     tables, held by every GPU that loads the library until the process exits;
-//   * one call may cover at most 64 MiB / (n_station * n_freq * 8) frames (21 at
-//     24 inputs and n_freq 16384); larger requests are rejected with
-//     CORR_ERR_ARG, nothing is launched, and the caller splits them;
-//   * the first call on a device looks up the arrays' device addresses
-//     (cudaGetSymbolAddress) with that device current; make that first call
+//   * one call may cover at most 64 MiB / (n_station * n_freq * e) frames, e the
+//     bytes a spectrum bin takes between the engines (4 for the FP16 tensor
+//     X-engine, 8 for the plain and split forms): 42 or 21 frames at 24 inputs
+//     and n_freq 16384. Larger requests are rejected with CORR_ERR_ARG, nothing
+//     is launched, and the caller splits them;
+//   * the first call on a device does that device's set-up with it current: it
+//     looks up the arrays' device addresses (cudaGetSymbolAddress) and copies
+//     the twiddle tables into theirs (synchronous copies). Make that first call
 //     before any stream capture;
-//   * every call shares the arrays: two calls whose kernels overlap on the GPU
-//     (different streams, no ordering between them) race on the scratch and
-//     give wrong results. Calls on one stream are ordered and safe. Nothing has
+//   * every call shares the spectra array: two calls whose kernels overlap on
+//     the GPU (different streams, no ordering between them) race on it and give
+//     wrong results. Calls on one stream are ordered and safe. Nothing in it has
 //     to start at zero: each call writes every scratch value it reads;
 //   * a bounded wait that runs out inside a kernel ends that kernel early
 //     without a report (there is no engine to hold a watchdog flag); use
 //     corrx_accumulate where that report matters.
 
-#include <cmath>
 #include <mutex>
+#include <vector>
 
 #include "engine.h"
 
@@ -36,9 +39,13 @@ namespace corrgb {
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;
-constexpr int kMaxFreq = 16384;
-constexpr int kTwEntries = 64 + kMaxFreq / 64 + 64 + kMaxFreq / 64;
-constexpr int kMaxDevices = 64;
+constexpr int kMinLogFreq = 9, kMaxLogFreq = 14;   // n_freq 512 .. 16384
+
+// Offset of the twiddle tables of 2^l channels in the twiddle array.
+constexpr int twiddle_offset(int l) {
+    return l == kMinLogFreq ? 0 : twiddle_offset(l - 1) + twiddle_entries(1 << (l - 1));
+}
+constexpr int kTwEntries = twiddle_offset(kMaxLogFreq + 1);
 
 static __device__ __align__(256) float2 g_noalloc_spectra[kNoAllocScratchBytes / sizeof(float2)];
 static __device__ __align__(256) float2 g_noalloc_twiddles[kTwEntries];
@@ -51,11 +58,13 @@ struct DeviceScratch {
 };
 
 std::mutex g_mu;
-DeviceScratch g_dev[kMaxDevices];
+DeviceScratch g_dev[kMaxDeviceOrdinals];
 
-// Device addresses of the scratch arrays on `dev` (current), looked up once.
+// Set-up of `dev` (the current device), once: the arrays' device addresses, the
+// SM count, and the twiddle tables of every supported length.
 corr_status scratch_for(int dev, DeviceScratch *out) {
-    if (dev < 0 || dev >= kMaxDevices) return failf(CORR_ERR_ARG, "device %d out of range", dev);
+    if (dev < 0 || dev >= kMaxDeviceOrdinals)
+        return failf(CORR_ERR_ARG, "device %d out of range", dev);
     std::lock_guard<std::mutex> lock(g_mu);
     DeviceScratch &d = g_dev[dev];
     if (!d.ready) {
@@ -68,6 +77,15 @@ corr_status scratch_for(int dev, DeviceScratch *out) {
                         "cudaGetSymbolAddress(twiddle scratch)");
         if (st != CORR_OK) return st;
         d.twiddles = static_cast<float2 *>(p);
+        std::vector<float2> all, tab;
+        for (int l = kMinLogFreq; l <= kMaxLogFreq; ++l) {
+            fengine_twiddles_host(1 << l, &tab);
+            all.insert(all.end(), tab.begin(), tab.end());
+        }
+        st = cuda_check(cudaMemcpy(d.twiddles, all.data(), all.size() * sizeof(float2),
+                                   cudaMemcpyHostToDevice),
+                        "cudaMemcpy(twiddle scratch)");
+        if (st != CORR_OK) return st;
         st = cuda_check(cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, dev),
                         "cudaDeviceGetAttribute(SM count)");
         if (st != CORR_OK) return st;
@@ -75,23 +93,6 @@ corr_status scratch_for(int dev, DeviceScratch *out) {
     }
     *out = d;
     return CORR_OK;
-}
-
-// The F-engine's four twiddle tables (layout of TwiddleTables, engine.h) for
-// transform length M, in double precision rounded once to float.
-__global__ void noalloc_twiddle_kernel(float2 *tw, int M) {
-    const int n_hi = M / 64;
-    const int total = 64 + n_hi + 64 + n_hi;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        double x;   // angle / pi
-        if (i < 64) x = -2.0 * i / M;                                   // pass_lo
-        else if (i < 64 + n_hi) x = -2.0 * 64.0 * (i - 64) / M;          // pass_hi
-        else if (i < 128 + n_hi) x = -1.0 * (i - 64 - n_hi) / M;          // post_lo
-        else x = -64.0 * (i - 128 - n_hi) / M;                           // post_hi
-        double s, c;
-        sincospi(x, &s, &c);
-        tw[i] = make_float2(static_cast<float>(c), static_cast<float>(s));
-    }
 }
 
 } // namespace
@@ -115,13 +116,15 @@ extern "C" corr_status corrx_accumulate_noalloc(int32_t n_station, int32_t n_fre
         return fail(CORR_ERR_ARG, "frame_stride is shorter than a frame");
     if ((reinterpret_cast<uintptr_t>(d_samples) | station_stride | frame_stride) % 16 != 0)
         return fail(CORR_ERR_ARG, "samples, station_stride and frame_stride must be 16-byte aligned");
-    const size_t per_frame = static_cast<size_t>(n_station) * n_freq * sizeof(float2);
+    // bytes a bin takes between the engines: FP16 pairs, or 8-byte FP32 / hi-lo pairs
+    const size_t bin_bytes = spectra_format(xmode) == kSpectraF16 ? 4 : 8;
+    const size_t per_frame = static_cast<size_t>(n_station) * n_freq * bin_bytes;
     const int max_frames = static_cast<int>(kNoAllocScratchBytes / per_frame);
     if (frames > max_frames)
         return failf(CORR_ERR_ARG,
                      "frames=%d exceeds the %d frames the fixed %zu-byte scratch holds at "
-                     "n_station=%d, n_freq=%d; split the call",
-                     frames, max_frames, kNoAllocScratchBytes, n_station, n_freq);
+                     "n_station=%d, n_freq=%d, X-engine mode %d; split the call",
+                     frames, max_frames, kNoAllocScratchBytes, n_station, n_freq, xmode);
     if (frames == 0) return CORR_OK;
 
     int dev = 0;
@@ -130,15 +133,10 @@ extern "C" corr_status corrx_accumulate_noalloc(int32_t n_station, int32_t n_fre
     if ((st = scratch_for(dev, &d)) != CORR_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
-    noalloc_twiddle_kernel<<<4, 256, 0, s>>>(d.twiddles, n_freq);
-    if ((st = cuda_check(cudaGetLastError(), "noalloc_twiddle_kernel launch")) != CORR_OK) return st;
+    int l = 0;
+    while ((1 << l) < n_freq) ++l;
     TwiddleTables tw;
-    tw.n_pass_hi = n_freq / 64;
-    tw.n_post_hi = n_freq / 64;
-    tw.pass_lo = d.twiddles;
-    tw.pass_hi = tw.pass_lo + 64;
-    tw.post_lo = tw.pass_hi + tw.n_pass_hi;
-    tw.post_hi = tw.post_lo + 64;
+    twiddle_views(d.twiddles + twiddle_offset(l), n_freq, &tw);
 
     FengineArgs fa{};
     fa.samples = d_samples;
@@ -166,7 +164,8 @@ extern "C" corr_status corrx_accumulate_noalloc(int32_t n_station, int32_t n_fre
     xa.n_station = n_station;
     xa.n_freq = n_freq;
     xa.frames = frames;
-    xa.acc = static_cast<float2 *>(d_acc);
+    xa.acc = d_acc;
+    xa.acc64 = 0;
     xa.err = nullptr;
     if (xmode == CORR_X_PLAIN_FP32) return xengine_plain_launch(xa, d.num_sms, s);
     int ct = 0, kt = 0;

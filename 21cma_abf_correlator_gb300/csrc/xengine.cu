@@ -40,8 +40,8 @@ __device__ __forceinline__ void decode_pair(int p, int nb, int *bj, int *bk) {
 
 __global__ void __launch_bounds__(1024, 1)
     xengine_plain_kernel(const float2 *__restrict__ y, int y_frames, int ytile, int n_station,
-                         int npad, int n_freq, int frames, float2 *__restrict__ acc,
-                         int pairs_per_cta, int n_pairs) {
+                         int npad, int n_freq, int frames, void *__restrict__ acc,
+                         int acc64, int pairs_per_cta, int n_pairs) {
     extern __shared__ __align__(16) float2 xs[];   // [stage][frame][npad][32]
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -127,11 +127,20 @@ __global__ void __launch_bounds__(1024, 1)
             const int k = bk * kBlk + l;
             if (j <= k && k < n_station) {
                 const int b = j * n_station - j * (j - 1) / 2 + (k - j);
-                float2 *dst = acc + static_cast<size_t>(b) * n_freq + c;
-                float2 v = *dst;
-                v.x += a[i][l].x;
-                v.y += a[i][l].y;
-                *dst = v;
+                const size_t at = static_cast<size_t>(b) * n_freq + c;
+                if (acc64) {   // complex128 row: the launch's FP32 sum added in double
+                    double2 *dst = static_cast<double2 *>(acc) + at;
+                    double2 v = *dst;
+                    v.x += a[i][l].x;
+                    v.y += a[i][l].y;
+                    *dst = v;
+                } else {
+                    float2 *dst = static_cast<float2 *>(acc) + at;
+                    float2 v = *dst;
+                    v.x += a[i][l].x;
+                    v.y += a[i][l].y;
+                    *dst = v;
+                }
             }
         }
     }
@@ -145,6 +154,58 @@ __global__ void scale_kernel(float2 *__restrict__ acc, size_t n, float s) {
         v.x *= s;
         v.y *= s;
         acc[i] = v;
+    }
+}
+
+__global__ void scale64_kernel(double2 *__restrict__ acc, size_t n, double s) {
+    const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+    for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += stride) {
+        double2 v = acc[i];
+        v.x *= s;
+        v.y *= s;
+        acc[i] = v;
+    }
+}
+
+__global__ void add64_kernel(double2 *__restrict__ dst, const double2 *__restrict__ src,
+                             size_t n) {
+    const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+    for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += stride) {
+        double2 v = dst[i];
+        const double2 w = src[i];
+        v.x += w.x;
+        v.y += w.y;
+        dst[i] = v;
+    }
+}
+
+// Two channels per thread: 32 bytes of complex128 in, 16 bytes of complex64 out.
+__global__ void dump64_kernel(float2 *__restrict__ out, size_t out_row,
+                              const double2 *__restrict__ src, size_t src_row,
+                              const int32_t *__restrict__ gmap, const int32_t *__restrict__ lmap,
+                              int n_map, int half_freq, int rows, double s) {
+    const size_t per_row = static_cast<size_t>(n_map) * half_freq;
+    const size_t n = per_row * rows;
+    const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+    for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += stride) {
+        const int r = static_cast<int>(i / per_row);
+        const size_t q = i - static_cast<size_t>(r) * per_row;
+        const int m = static_cast<int>(q / half_freq);
+        const int c2 = static_cast<int>(q - static_cast<size_t>(m) * half_freq);
+        const int gb = gmap ? gmap[m] : m;
+        const int lb = lmap ? lmap[m] : m;
+        const double2 *a = src + r * src_row + (static_cast<size_t>(lb) * half_freq + c2) * 2;
+        const double2 a0 = a[0], a1 = a[1];
+        float4 v;
+        v.x = static_cast<float>(a0.x * s);
+        v.y = static_cast<float>(a0.y * s);
+        v.z = static_cast<float>(a1.x * s);
+        v.w = static_cast<float>(a1.y * s);
+        *reinterpret_cast<float4 *>(out + r * out_row +
+                                    (static_cast<size_t>(gb) * half_freq + c2) * 2) = v;
     }
 }
 
@@ -191,18 +252,18 @@ corr_status xengine_plain_launch(const XengineArgs &a, int num_sms, cudaStream_t
     const int groups = (n_pairs + 31) / 32;
     const int per_cta = (n_pairs + groups - 1) / groups;
     const size_t smem = static_cast<size_t>(kXstages) * kXfs * npad * kXch * sizeof(float2);
-    static bool configured = false;
-    if (!configured) {
-        corr_status st = cuda_check(
-            cudaFuncSetAttribute(xengine_plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 227 * 1024),
-            "cudaFuncSetAttribute(xengine_plain)");
-        if (st != CORR_OK) return st;
-        configured = true;
-    }
+    static PerDevice setup;   // the shared-memory limit is a per-device setting
+    corr_status st = setup.run([](int) {
+        return cuda_check(cudaFuncSetAttribute(xengine_plain_kernel,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               227 * 1024),
+                          "cudaFuncSetAttribute(xengine_plain)");
+    });
+    if (st != CORR_OK) return st;
     dim3 grid(groups, a.n_freq / kXch);
     xengine_plain_kernel<<<grid, per_cta * 32, smem, stream>>>(
-        a.y, a.y_frames, a.ytile, a.n_station, npad, a.n_freq, a.frames, a.acc, per_cta, n_pairs);
+        a.y, a.y_frames, a.ytile, a.n_station, npad, a.n_freq, a.frames, a.acc, a.acc64, per_cta,
+        n_pairs);
     return cuda_check(cudaGetLastError(), "xengine_plain_kernel launch");
 }
 
@@ -212,6 +273,37 @@ corr_status scale_launch(float2 *acc, size_t n, float s, cudaStream_t stream) {
     if (blocks > 4096) blocks = 4096;
     scale_kernel<<<static_cast<unsigned>(blocks), 256, 0, stream>>>(acc, n, s);
     return cuda_check(cudaGetLastError(), "scale_kernel launch");
+}
+
+namespace {
+unsigned grid_for(size_t n, unsigned cap) {
+    size_t blocks = (n + 255) / 256;
+    if (blocks > cap) blocks = cap;
+    return static_cast<unsigned>(blocks < 1 ? 1 : blocks);
+}
+} // namespace
+
+corr_status scale64_launch(double2 *acc, size_t n, double s, cudaStream_t stream) {
+    if (n == 0) return CORR_OK;
+    scale64_kernel<<<grid_for(n, 4096), 256, 0, stream>>>(acc, n, s);
+    return cuda_check(cudaGetLastError(), "scale64_kernel launch");
+}
+
+corr_status add64_launch(double2 *dst, const double2 *src, size_t n, cudaStream_t stream) {
+    if (n == 0) return CORR_OK;
+    add64_kernel<<<grid_for(n, 4096), 256, 0, stream>>>(dst, src, n);
+    return cuda_check(cudaGetLastError(), "add64_kernel launch");
+}
+
+corr_status dump64_launch(float2 *out, size_t out_row, const double2 *src, size_t src_row,
+                          const int32_t *gmap, const int32_t *lmap, int n_map, int n_freq,
+                          int rows, double s, cudaStream_t stream) {
+    if (n_freq % 2 != 0) return fail(CORR_ERR_INTERNAL, "dump64: n_freq must be even");
+    const size_t n = static_cast<size_t>(n_map) * (n_freq / 2) * static_cast<size_t>(rows);
+    if (n == 0) return CORR_OK;
+    dump64_kernel<<<grid_for(n, 4096), 256, 0, stream>>>(out, out_row, src, src_row, gmap, lmap,
+                                                          n_map, n_freq / 2, rows, s);
+    return cuda_check(cudaGetLastError(), "dump64_kernel launch");
 }
 
 // MurmurHash3's 32-bit finaliser (a published integer mixing function).

@@ -87,6 +87,9 @@ constexpr int kMaxLoadStages = 6;
 constexpr int kMaxOpStages = 3;
 constexpr int kMaxItems = 4;                     // conversion items per converter thread
 constexpr int kLBO = 128;                        // bytes between K-adjacent core matrices
+// Dynamic shared memory of any feasible shape: the 227 KB a CTA may opt into,
+// less 1 KB left for the kernel's static shared variables.
+constexpr int kMaxSmem = 227 * 1024 - 1024;
 
 enum TcForm : int { kSplitStacked = 0, kSplitWide = 1, kFp16Paired = 2, kFp16Wide = 3 };
 
@@ -191,7 +194,7 @@ TcGeom make_geom(int n_station, bool split, int ct, int kt) {
     g.vs_bytes = round_up(n_baseline * ct * 8, 128);
     g.qs_bytes = split ? round_up(N * N * ct * 8, 128) : 0;
     const int jk_bytes = round_up(n_baseline * 2, 128);
-    const int budget = 227 * 1024 - 1024;
+    const int budget = kMaxSmem;
     const int fixed = g.vs_bytes + g.qs_bytes + jk_bytes + 128;
     g.n_op = 2;
     if (fixed + g.n_op * g.op_stage + 2 * g.ld_stage > budget) return g;
@@ -283,7 +286,8 @@ struct TcParams {
     int n_station;
     int n_freq;
     int frames;
-    float2 *acc;
+    void *acc;         // float2 row, or double2 row when acc64
+    int acc64;
     int *err;
     float inv_scale2;  // 1/scale^2: undoes the F-engine's spectra scale in S
     TcGeom g;
@@ -693,44 +697,79 @@ __global__ void __launch_bounds__(kThreads, 1)
             // Four read-modify-writes per thread in flight: all loads first.
             constexpr int kBatch = 4;
             const int n_items = n_baseline * nq;
-            for (int q0 = et; q0 < n_items; q0 += kEpilogue * kBatch) {
-                float4 a[kBatch];
-                float4 *dst[kBatch];
+            // visibilities of channels c, c+1 of item q's baseline
+            auto vis = [&](int q, float2 &v0, float2 &v1) {
+                const int b = q / nq;
+                const int c = (q - b * nq) * 2;
+                const int j = jk[b] >> 8, k = jk[b] & 0xff;
+                const int tri = k * (k + 1) / 2 + j;
+                v0 = Vs[c * plane_v + tri];
+                v1 = Vs[(c + 1) * plane_v + tri];
+                if (g.split) {
+                    const float2 qa0 = Qs[(c * N + k) * N + j], qb0 = Qs[(c * N + j) * N + k];
+                    const float2 qa1 = Qs[((c + 1) * N + k) * N + j];
+                    const float2 qb1 = Qs[((c + 1) * N + j) * N + k];
+                    v0.x += qa0.x + qb0.x;
+                    v0.y += qa0.y - qb0.y;
+                    v1.x += qa1.x + qb1.x;
+                    v1.y += qa1.y - qb1.y;
+                }
+            };
+            auto row_offset = [&](int q) {
+                const int b = q / nq;
+                const int c = (q - b * nq) * 2;
+                return static_cast<size_t>(b) * p.n_freq + c0 + c;
+            };
+            if (p.acc64) {
+                // complex128 row: the launch's FP32 sums are added in double
+                double2 *acc = static_cast<double2 *>(p.acc);
+                for (int q0 = et; q0 < n_items; q0 += kEpilogue * kBatch) {
+                    double2 a[kBatch][2];
 #pragma unroll
-                for (int u = 0; u < kBatch; ++u) {
-                    const int q = q0 + u * kEpilogue;
-                    dst[u] = nullptr;
-                    if (q < n_items) {
-                        const int b = q / nq;
-                        const int c = (q - b * nq) * 2;
-                        dst[u] = reinterpret_cast<float4 *>(p.acc + static_cast<size_t>(b) * p.n_freq +
-                                                            c0 + c);
-                        a[u] = *dst[u];
+                    for (int u = 0; u < kBatch; ++u) {
+                        const int q = q0 + u * kEpilogue;
+                        if (q < n_items) {
+                            const double2 *src = acc + row_offset(q);
+                            a[u][0] = src[0];
+                            a[u][1] = src[1];
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < kBatch; ++u) {
+                        const int q = q0 + u * kEpilogue;
+                        if (q >= n_items) break;
+                        float2 v0, v1;
+                        vis(q, v0, v1);
+                        a[u][0].x += v0.x;
+                        a[u][0].y += v0.y;
+                        a[u][1].x += v1.x;
+                        a[u][1].y += v1.y;
+                        double2 *dst = acc + row_offset(q);
+                        dst[0] = a[u][0];
+                        dst[1] = a[u][1];
                     }
                 }
+            } else {
+                float2 *acc = static_cast<float2 *>(p.acc);
+                for (int q0 = et; q0 < n_items; q0 += kEpilogue * kBatch) {
+                    float4 a[kBatch];
 #pragma unroll
-                for (int u = 0; u < kBatch; ++u) {
-                    const int q = q0 + u * kEpilogue;
-                    if (q >= n_items) break;
-                    const int b = q / nq;
-                    const int c = (q - b * nq) * 2;
-                    const int j = jk[b] >> 8, k = jk[b] & 0xff;
-                    const int tri = k * (k + 1) / 2 + j;
-                    float2 v0 = Vs[c * plane_v + tri], v1 = Vs[(c + 1) * plane_v + tri];
-                    if (g.split) {
-                        const float2 qa0 = Qs[(c * N + k) * N + j], qb0 = Qs[(c * N + j) * N + k];
-                        const float2 qa1 = Qs[((c + 1) * N + k) * N + j];
-                        const float2 qb1 = Qs[((c + 1) * N + j) * N + k];
-                        v0.x += qa0.x + qb0.x;
-                        v0.y += qa0.y - qb0.y;
-                        v1.x += qa1.x + qb1.x;
-                        v1.y += qa1.y - qb1.y;
+                    for (int u = 0; u < kBatch; ++u) {
+                        const int q = q0 + u * kEpilogue;
+                        if (q < n_items) a[u] = *reinterpret_cast<const float4 *>(acc + row_offset(q));
                     }
-                    a[u].x += v0.x;
-                    a[u].y += v0.y;
-                    a[u].z += v1.x;
-                    a[u].w += v1.y;
-                    *dst[u] = a[u];
+#pragma unroll
+                    for (int u = 0; u < kBatch; ++u) {
+                        const int q = q0 + u * kEpilogue;
+                        if (q >= n_items) break;
+                        float2 v0, v1;
+                        vis(q, v0, v1);
+                        a[u].x += v0.x;
+                        a[u].y += v0.y;
+                        a[u].z += v1.x;
+                        a[u].w += v1.y;
+                        *reinterpret_cast<float4 *>(acc + row_offset(q)) = a[u];
+                    }
                 }
             }
             // everyone done with Vs/Qs before the next tile overwrites them
@@ -896,15 +935,16 @@ corr_status xengine_tc_launch(const XengineArgs &a, bool split, int ct, int kt, 
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (cr != CUDA_SUCCESS)
         return failf(CORR_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", static_cast<int>(cr));
-    static int configured_smem = 0;
-    if (configured_smem < g.smem) {
-        corr_status st = cuda_check(
-            cudaFuncSetAttribute(xengine_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 g.smem),
-            "cudaFuncSetAttribute(xengine_tc)");
-        if (st != CORR_OK) return st;
-        configured_smem = g.smem;
-    }
+    // The shared-memory limit is a per-device setting: raise it once on each
+    // device to the most any feasible shape uses (kMaxSmem), not per shape.
+    static PerDevice setup;
+    corr_status st = setup.run([](int) {
+        return cuda_check(cudaFuncSetAttribute(xengine_tc_kernel,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               kMaxSmem),
+                          "cudaFuncSetAttribute(xengine_tc)");
+    });
+    if (st != CORR_OK) return st;
     TcParams p{};
     p.ytile = a.ytile;
     p.bulk = a.ytile == g.ct;
@@ -917,6 +957,7 @@ corr_status xengine_tc_launch(const XengineArgs &a, bool split, int ct, int kt, 
     p.n_freq = a.n_freq;
     p.frames = a.frames;
     p.acc = a.acc;
+    p.acc64 = a.acc64;
     p.err = a.err;
     const float scale = spectra_scale(a.n_freq);   // applied by the F-engine
     p.inv_scale2 = 1.0f / (scale * scale);

@@ -53,9 +53,28 @@ class FxEngine:
         except Exception:
             pass
 
+    def set_accumulator(self, precision: int) -> None:
+        """abi.CORRX_ACC_FP32 (complex64 rows, the default) or abi.CORRX_ACC_FP64
+        (complex128 rows: each launch's FP32 sums are added in double)."""
+        abi.check(self.lib.corrx_set_accumulator(self.h, precision), "corrx_set_accumulator")
+        self.acc64 = precision == abi.CORRX_ACC_FP64
+
     def new_acc(self):
+        """A zeroed row in the engine's accumulator precision."""
         import torch
-        return torch.zeros((self.n_baseline, self.n_freq), dtype=torch.complex64, device="cuda")
+        dt = torch.complex128 if getattr(self, "acc64", False) else torch.complex64
+        return torch.zeros((self.n_baseline, self.n_freq), dtype=dt, device="cuda")
+
+    def dump(self, acc, frames: int, out=None, stream=None):
+        """complex64 row = acc / frames (rounded once); returns `out`."""
+        import torch
+        if out is None:
+            out = torch.empty((self.n_baseline, self.n_freq), dtype=torch.complex64,
+                              device=acc.device)
+        abi.check(self.lib.corrx_dump(self.h, C.c_void_p(acc.data_ptr()), frames,
+                                      C.c_void_p(out.data_ptr()),
+                                      C.c_void_p(_stream_handle(stream))), "corrx_dump")
+        return out
 
     def accumulate(self, samples, frames: int, acc, mask=None, mask_bit0: int = 0,
                    stream=None, frame0: int = 0, packets=None, packets_frame0: int = 0) -> None:

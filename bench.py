@@ -278,11 +278,14 @@ def main() -> None:
     stream = torch.cuda.current_stream()
     samples_step = N * F * L
 
-    def make_step(eng, acc):
+    def make_step(eng, acc, row):
+        # the integration accumulates in complex128 (FP64 cross-launch
+        # accumulator) and is dumped, divided by its frame count, into a
+        # complex64 row
         def step():
             acc.zero_()
             eng.accumulate(x, F, acc, mask=mask, stream=stream)
-            eng.scale(acc, F, stream=stream)
+            eng.dump(acc, F, row, stream=stream)
         return step
 
     results = {}
@@ -300,8 +303,10 @@ def main() -> None:
                 tiles[name] = eng.tiles()
             else:
                 tiles[name] = eng.autotune(stream)
+            eng.set_accumulator(abi.CORRX_ACC_FP64)
             acc = eng.new_acc()
-            step = make_step(eng, acc)
+            row = torch.empty((B, nf), dtype=torch.complex64, device="cuda")
+            step = make_step(eng, acc, row)
             step()
             torch.cuda.synchronize()
             eng.check()
@@ -309,7 +314,7 @@ def main() -> None:
             if e.status == abi.CORR_ERR_NOT_IMPL:
                 continue
             raise
-        engines[name] = (eng, acc, step)
+        engines[name] = (eng, acc, step, row)
     if not engines:
         raise SystemExit("no X-engine available")
     # FFT plan 2 (the tensor-core F-engine, n_freq 16384, FP16 spectra) on the FP16
@@ -320,12 +325,14 @@ def main() -> None:
         eng = pkg.FxEngine(N, nf, PASS_FRAMES, xmode=modes["tc"])
         eng.set_tiles(t_["ytile"], t_["xct"], t_["xkt"], 2)
         tiles["tc_tensor_fft"] = eng.tiles()
+        eng.set_accumulator(abi.CORRX_ACC_FP64)
         acc = eng.new_acc()
-        step = make_step(eng, acc)
+        row = torch.empty((B, nf), dtype=torch.complex64, device="cuda")
+        step = make_step(eng, acc, row)
         step()
         torch.cuda.synchronize()
         eng.check()
-        engines["tc_tensor_fft"] = (eng, acc, step)
+        engines["tc_tensor_fft"] = (eng, acc, step, row)
         err_bound["tc_tensor_fft"] = err_bound["tc"]
 
     def time_steps(step, k, w_):
@@ -345,15 +352,30 @@ def main() -> None:
             torch.distributed.barrier()
         return e0.elapsed_time(e1) / k
 
-    # the headline path: the fastest X-engine whose tested error bound meets the
-    # 1e-4 precision target at this integration length
+    # rows of each path for this integration (identical input every step), and
+    # their errors against float64 over the whole row
+    accuracy = None
+    if rank == 0 and not args.no_accuracy:
+        rows = {name: e_[3].clone() for name, e_ in engines.items()}
+        accuracy = accuracy_report(torch, w, x, mask, rows)
+        del rows
+        torch.cuda.empty_cache()
+
+    # the headline path: the fastest X-engine that meets the 1e-4 precision
+    # target -- every visibility's error within 1e-4 of its two inputs' power
+    # (and the row's rel. RMS within 1e-4) -- as measured over the whole row
+    # against float64, or by its tested bound when no measurement was made
+    def meets(name):
+        if accuracy is not None and name in accuracy["vs_fp64_full_row"]:
+            e = accuracy["vs_fp64_full_row"][name]
+            return e["max_per_vis"] <= 1e-4 and e["rel_rms"] <= 1e-4
+        return err_bound[name] <= 1e-4
     per_path = {}
-    for name, (eng, acc, step) in engines.items():
-        per_path[name] = time_steps(step, 2, 1)
-    eligible = [n for n in per_path if err_bound[n] <= 1e-4 and n != "tc_tensor_fft"] \
-        or list(per_path)
+    for name, e_ in engines.items():
+        per_path[name] = time_steps(e_[2], 2, 1)
+    eligible = [n for n in per_path if meets(n) and n != "tc_tensor_fft"] or list(per_path)
     best = min(eligible, key=per_path.get)
-    eng, acc, step = engines[best]
+    eng, acc, step, row = engines[best]
 
     sampler = ClockSampler(local)
     sampler.start()
@@ -367,18 +389,27 @@ def main() -> None:
     value = replicas.job_gsps(samples_step, world, ms)
 
     paths = {}
-    for name, (e_, a_, s_) in engines.items():
-        m = ms if name == best else time_steps(s_, max(2, args.steps // 2), 1)
+    for name, e_ in engines.items():
+        m = ms if name == best else time_steps(e_[2], max(2, args.steps // 2), 1)
         paths[name] = {"value": samples_step / (m * 1e-3) / 1e9, "ms_per_step": m,
                        "tiles": {k: tiles[name][k] for k in ("ytile", "xct", "xkt", "fplan")},
-                       "per_vis_err_bound": err_bound[name]}
+                       "per_vis_err_bound": err_bound[name], "meets_1e-4": meets(name)}
 
-    # rows of each path for the integration just timed (identical input every step)
-    accuracy = None
-    if rank == 0 and not args.no_accuracy:
-        rows = {name: a_.clone() for name, (e_, a_, s_) in engines.items()}
-        accuracy = accuracy_report(torch, w, x, mask, rows)
-        del rows
+    # what the FP64 cross-launch accumulator costs: the headline path with a
+    # complex64 accumulator instead (scaled in place, no dump)
+    acc32 = torch.zeros((B, nf), dtype=torch.complex64, device="cuda")
+    eng.set_accumulator(abi.CORRX_ACC_FP32)
+
+    def step32():
+        acc32.zero_()
+        eng.accumulate(x, F, acc32, mask=mask, stream=stream)
+        eng.scale(acc32, F, stream=stream)
+    ms32 = time_steps(step32, max(2, args.steps // 2), 1)
+    eng.set_accumulator(abi.CORRX_ACC_FP64)
+    del acc32
+    accumulator = {"precision": "fp64 (complex128 row; each launch's FP32 sums added once)",
+                   "ms_per_step_fp64": ms, "ms_per_step_fp32": ms32,
+                   "cost_ms_per_integration": ms - ms32}
 
     # per-kernel times: one pass of PASS_FRAMES frames through each kernel alone
     hbm_peak, _, peak_kind = peaks()
@@ -413,7 +444,8 @@ def main() -> None:
     mb = synth.mask_bytes(F) if mask is not None else 0
     elem = 4 if best == "tc" else 8   # bytes per spectrum bin between the engines
     f_bytes = N * PASS_FRAMES * L + N * PASS_FRAMES * nf * elem + (N * mb * PASS_FRAMES // F)
-    x_bytes = N * PASS_FRAMES * nf * elem + 2 * B * nf * 8
+    # spectra read once + the complex128 row read and written once per launch
+    x_bytes = N * PASS_FRAMES * nf * elem + 2 * B * nf * 16
     # Nominal arithmetic of a length-L real FFT (half-length complex FFT + split):
     # 2.5 L log2 L flops. The FP32 peak is nominal (no measured figure on file):
     # SMs x 128 FMA lanes x 2 flops x the maximum SM clock.
@@ -436,9 +468,10 @@ def main() -> None:
     roofline = {"kernel": dom, "bound": "hbm", "achieved": dk["achieved_gbs"],
                 "peak": hbm_peak, "unit": "GB/s", "frac": dk["achieved_gbs"] / hbm_peak,
                 "peak_kind": peak_kind,
-                "traffic": ncu_traffic(dom, w.name, PASS_FRAMES, best),
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a "
-                                  "256-frame launch, scaled to frames_per_launch",
+                "traffic": ncu_traffic(dom, w.name, PASS_FRAMES, best, paths[best]["tiles"]),
+                "traffic_source": "profiles/traffic.json: ncu dram__bytes_read.sum + "
+                                  "dram__bytes_write.sum of one captured launch, scaled to "
+                                  "frames_per_launch",
                 "alg_bytes_per_launch": dk["alg_bytes"], "frames_per_launch": PASS_FRAMES}
     if dom == "fengine":
         roofline["limiter"] = ("FP32 FFT arithmetic and shared-memory exchanges, not HBM: ncu on a "
@@ -474,7 +507,8 @@ def main() -> None:
 
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
-        cpu = time_cpu_oracle(w, args.cpu_seconds, 1)
+        # the reference's CPU formulation on every host core, as the reference arm runs it
+        cpu = time_cpu_oracle(w, args.cpu_seconds, os.cpu_count() or 1)
         cpu["kind"] = "port"
 
     passes = math.ceil(F / PASS_FRAMES)
@@ -492,6 +526,7 @@ def main() -> None:
                        "frames_per_pass": PASS_FRAMES, "parallelism": f"replicas x{world}",
                        "l2": f"inputs {N * F * L / 1e9:.2f} GB per step > L2; no flush"},
             "paths": paths, "kernels": kernels, "roofline": roofline, "accuracy": accuracy,
+            "accumulator": accumulator,
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
             "gpu_launches": launches_per_step * args.steps,
         }
@@ -501,25 +536,21 @@ def main() -> None:
         torch.distributed.destroy_process_group()
 
 
-# DRAM bytes per launch of the precision workload's kernels (24 inputs, n_freq
-# 16384), per X-engine path, from one ncu capture of 256-frame launches
-# (profiles/*_precision-24in-nf16384.md), scaled by frames: the F-engine's
-# traffic is all per frame (int8 read, spectra write); the X-engines' is the
-# spectra read (per frame) plus the row's read and write (per launch).
-_NCU_256 = {
-    "fengine": {"tc": (543.339520e6, 0.0), "tc_split": (944.290816e6, 0.0),
-                "plain": (944.951296e6, 0.0)},
-    "xengine": {"tc": (402.653184e6, 69.594368e6), "tc_split": (805.306368e6, 74.313728e6),
-                "plain": (805.306368e6, 73.831936e6)},
-}
-
-
-def ncu_traffic(kernel: str, workload: str, frames: int, path: str):
-    entry = _NCU_256["fengine" if kernel == "fengine" else "xengine"].get(path)
-    if workload != "precision-24in-nf16384" or entry is None:
+def ncu_traffic(kernel: str, workload: str, frames: int, path: str, tiles: dict):
+    """DRAM bytes per launch of `kernel` on this workload and path, from the ncu
+    captures summarised in profiles/traffic.json: bytes_per_frame * frames +
+    bytes_per_launch (the F-engine's traffic is all per frame -- int8 read,
+    spectra written; the X-engines' is the spectra read per frame plus the row's
+    read and write per launch). None when no capture matches the configuration."""
+    p = REPO / "profiles" / "traffic.json"
+    if not p.exists():
         return None
-    per, fixed = entry
-    return per * frames / 256 + fixed
+    kind = "fengine" if kernel == "fengine" else "xengine"
+    for e in json.loads(p.read_text()).get("captures", []):
+        if (e["workload"] == workload and e["kernel"] == kind and e["path"] == path
+                and e.get("fplan", 0) == tiles.get("fplan", 0)):
+            return e["bytes_per_frame"] * frames + e["bytes_per_launch"]
+    return None
 
 
 def run_batching(pkg, synth, torch, stream, forms) -> dict:
@@ -541,6 +572,7 @@ def run_batching(pkg, synth, torch, stream, forms) -> dict:
     for xmode, _, _ in forms:
         e_ = pkg.FxEngine(w.n_station, w.n_freq, PASS_FRAMES, xmode=xmode)
         e_.autotune(stream)
+        e_.set_accumulator(abi.CORRX_ACC_FP64)   # each block integrates in complex128
         engs.append(e_)
     which = [next(i for i, f in enumerate(forms) if b[1] >= f[2]) for b in plan]
     rows = torch.empty((nblk, w.n_baseline, w.n_freq), dtype=torch.complex64, device="cuda")
@@ -615,12 +647,14 @@ def run_stream(pkg, synth, torch, stream) -> dict:
     eng = pkg.FxEngine(w.n_station, w.n_freq, PASS_FRAMES,
                        xmode=pkg.abi.CORR_X_TC_FP16_SPLIT)
     tiles = eng.autotune(stream)
+    eng.set_accumulator(pkg.abi.CORRX_ACC_FP64)
     acc = eng.new_acc()
+    row = torch.empty((w.n_baseline, w.n_freq), dtype=torch.complex64, device="cuda")
 
     def step():
         acc.zero_()
         eng.accumulate(x, w.frames, acc, mask=mask, stream=stream)
-        eng.scale(acc, w.frames, stream=stream)
+        eng.dump(acc, w.frames, row, stream=stream)
     for _ in range(2):
         step()
     torch.cuda.synchronize()
@@ -633,12 +667,12 @@ def run_stream(pkg, synth, torch, stream) -> dict:
     eng.check()
     ms = e0.elapsed_time(e1) / 2
     # error of the first integration against the float64 DFT at 16 channels
-    acc_rep = accuracy_report(torch, w, x, mask, {"tc_split": acc.clone()})
+    acc_rep = accuracy_report(torch, w, x, mask, {"tc_split": row.clone()})
     # a 60-s stream's worth of integrations back to back (the input frames are a
     # resident pool reused per integration), each timed from its first launch
     # until its row is in pinned host memory
     n_int = math.ceil(60.0 * 250e6 / (w.frames * w.fft_len))
-    host_row = torch.empty(acc.shape, dtype=acc.dtype, pin_memory=True)
+    host_row = torch.empty(row.shape, dtype=row.dtype, pin_memory=True)
     marks = [torch.cuda.Event(enable_timing=True) for _ in range(n_int + 1)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(n_int)]
     marks[0].record(stream)
@@ -647,7 +681,7 @@ def run_stream(pkg, synth, torch, stream) -> dict:
             marks[i].record(stream)
         step()
         with torch.cuda.stream(stream):
-            host_row.copy_(acc, non_blocking=True)
+            host_row.copy_(row, non_blocking=True)
         ends[i].record(stream)
     marks[n_int].record(stream)
     torch.cuda.synchronize()
@@ -659,7 +693,7 @@ def run_stream(pkg, synth, torch, stream) -> dict:
     def step_packets():
         acc.zero_()
         eng.accumulate(x, w.frames, acc, stream=stream, packets=wd)
-        eng.scale(acc, w.frames, stream=stream)
+        eng.dump(acc, w.frames, row, stream=stream)
     step_packets()
     torch.cuda.synchronize()
     e0.record(stream)
@@ -669,7 +703,7 @@ def run_stream(pkg, synth, torch, stream) -> dict:
     torch.cuda.synchronize()
     eng.check()
     ms_pk = e0.elapsed_time(e1) / 2
-    acc_pk = accuracy_report(torch, w, x, None, {"tc_split": acc.clone()}, words=wd)
+    acc_pk = accuracy_report(torch, w, x, None, {"tc_split": row.clone()}, words=wd)
     # the F-engine alone on one pass: algorithmic HBM bytes / time
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     lib = eng.lib
@@ -707,7 +741,9 @@ def run_stream(pkg, synth, torch, stream) -> dict:
                         "frac_of_hbm": f_bytes / (t_f * 1e-3) / 1e9 / hbm, "peak_kind": kind},
             "accuracy_first_integration": {"channels": acc_rep["channels"],
                                            "baselines": acc_rep["baselines"],
-                                           "vs_fp64": acc_rep["vs_fp64"]["tc_split"]},
+                                           "vs_fp64": acc_rep["vs_fp64"]["tc_split"],
+                                           "vs_fp64_full_row":
+                                               acc_rep["vs_fp64_full_row"]["tc_split"]},
             "loss": f"{w.loss:.3%} of 1024-sample packets; frame-granular zero-fill (a frame "
                     f"with a lost packet is zeroed whole, the reference's rule)",
             "packet_granular": {
@@ -716,7 +752,9 @@ def run_stream(pkg, synth, torch, stream) -> dict:
                 "real_time_factor": w.n_station * w.frames * w.fft_len / (ms_pk * 1e-3) / 1e9
                 / need,
                 "loss": "only the lost packets zero-filled (corrx_accumulate_packets)",
-                "accuracy_first_integration_vs_fp64": acc_pk["vs_fp64"]["tc_split"]}}
+                "accuracy_first_integration_vs_fp64": acc_pk["vs_fp64"]["tc_split"],
+                "accuracy_first_integration_vs_fp64_full_row":
+                    acc_pk["vs_fp64_full_row"]["tc_split"]}}
 
 
 ACCURACY_CHANNELS = [0, 1, 2, 63, 1234, 2047, 3000, 4096, 5555, 8191, 8192, 9000, 12345,
@@ -780,16 +818,49 @@ def accuracy_report(torch, w, x, mask, rows: dict, channels=ACCURACY_CHANNELS,
                 "elementwise_count": int(big.sum())}
 
     chi = torch.tensor(ch, device=dev)
-    out = {"channels": ch, "baselines": len(pairs), "frames": F, "vs_fp64": {}, "vs_plain": {}}
+    out = {"channels": ch, "baselines": len(pairs), "frames": F, "vs_fp64": {}, "vs_plain": {},
+           "vs_fp64_full_row": {}}
     for name, r in rows.items():
         out["vs_fp64"][name] = errs(r[:, chi].to(torch.complex128), ref)
+    del Y, ref
+    # every visibility of the row against a float64 reference: float64 FFT of
+    # every frame (cuFFT through torch, a comparator only) and float64 sums
+    full = full_row_reference(torch, w, x, mask, words, jj, kk)
+    for name, r in rows.items():
+        out["vs_fp64_full_row"][name] = errs(r.to(torch.complex128), full)
+    out["full_row_reference"] = ("float64 rfft of every frame (torch.fft) and float64 "
+                                 "per-channel sums over all frames, every baseline and channel")
+    del full
     if "plain" in rows:
         p_ = rows["plain"].to(torch.complex128)
         for name, r in rows.items():
             if name != "plain":
                 out["vs_plain"][name] = errs(r.to(torch.complex128), p_)
-    del Y
     return out
+
+
+def full_row_reference(torch, w, x, mask, words, jj, kk, step: int = 128):
+    """complex128 [n_baseline, n_freq]: the integration's rows in float64."""
+    N, F, L, nf = w.n_station, w.frames, w.fft_len, w.n_freq
+    dev = x.device
+    G = torch.zeros((nf, N, N), dtype=torch.complex128, device=dev)
+    for f0 in range(0, F, step):
+        blk = x[:, f0:f0 + step].to(torch.float64)                       # [N, f, L]
+        f1 = f0 + blk.shape[1]
+        if mask is not None:
+            fr = torch.arange(f0, f1, device=dev)
+            bits = (mask[:, fr // 8].to(torch.int64) >> (fr % 8)) & 1     # [N, f]
+            blk *= bits.to(torch.float64)[:, :, None]
+        if words is not None:
+            P = L // 1024
+            wd = words[:, f0:f1].to(torch.int64)[:, :, None]
+            keep = ((wd >> torch.arange(P, device=dev)) & 1).to(torch.float64)   # [N, f, P]
+            blk = (blk.view(N, -1, P, 1024) * keep[..., None]).view(N, -1, L)
+        Y = torch.fft.rfft(blk, dim=-1)[..., :nf].permute(2, 0, 1)         # [nf, N, f]
+        del blk
+        G += Y @ Y.conj().transpose(1, 2)
+        del Y
+    return (G[:, jj, kk] / F).T.contiguous()
 
 
 def run_only(args) -> None:

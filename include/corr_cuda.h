@@ -43,8 +43,15 @@ extern "C" {
    device and cleared by corr_row_slot_free() (corr_cuda.h:94 in the reference). */
 #define CORR_ABI_VERSION 7u
 
-/* Split modes (reference corr_cuda.h:113-137). This library runs one device, on
-   which all three describe the same placement: every station, every baseline. */
+/* Split modes (reference corr_cuda.h:113-137): how a context with several
+   devices shares the work. TIME_SLICE routes slot sequence s to device
+   s % n_devices, each device holds every station and a partial row of every
+   baseline, and the fetch adds the partial rows. BASELINE_RANGE and
+   PAIR_COVERING copy every slot to every device; each device reports a set of
+   baselines (a contiguous range of them, over every station; or the baselines
+   among a subset of stations, each baseline on exactly one device) and the
+   fetch assembles the row. corrx_plan_query (corr_gb300.h) states the
+   placements exactly. */
 #define CORR_SPLIT_BASELINE_RANGE 0
 #define CORR_SPLIT_PAIR_COVERING 1
 #define CORR_SPLIT_TIME_SLICE 2
@@ -81,8 +88,8 @@ typedef enum corr_status {
  *       everything else CORR_ERR_ARG.
  *   frames_per_slot >= 1, 1 <= chunk_frames <= frames_per_slot
  *   block_slots >= 2, rows_per_fetch >= 1
- *   the device ordinal(s) exist and are distinct; more than one device is
- *       CORR_ERR_NOT_IMPL in this library
+ *   the device ordinal(s) exist and are distinct; the split gives every
+ *       device at least one baseline
  */
 typedef struct corr_config {
     uint32_t abi_version;

@@ -56,8 +56,9 @@ corr_status corrx_destroy(void *eng);
  * If d_mask is not NULL, frame f of station s is treated as all zeros unless bit
  * (mask_bit0 + f) of the bit string at d_mask + s*mask_station_stride is set
  * (LSB first), exactly as the staging validity mask is read.
- * d_acc holds n_baseline*n_freq complex64 (FP32 re, im), must not alias, and
- * must be 16-byte aligned for the tensor X-engines.
+ * d_acc holds n_baseline*n_freq complex64 (FP32 re, im), or complex128 for an
+ * engine with the FP64 accumulator (corrx_set_accumulator), must not alias, and
+ * must be 16-byte aligned.
  */
 corr_status corrx_accumulate(void *eng, const int8_t *d_samples, size_t station_stride,
                              size_t frame_stride, const uint8_t *d_mask,
@@ -80,8 +81,66 @@ corr_status corrx_accumulate_packets(void *eng, const int8_t *d_samples, size_t 
                                      int32_t pmask_frame0, int32_t frames, void *d_acc,
                                      void *stream);
 
-/* d_acc *= 1.0f/(float)frames over n_baseline*n_freq complex values. */
+/* d_acc *= 1.0f/(float)frames over n_baseline*n_freq complex values (in double
+   precision for an engine with the FP64 accumulator). */
 corr_status corrx_scale(void *eng, void *d_acc, uint64_t frames, void *stream);
+
+/*
+ * Accumulator precision of an engine. Every X-engine launch sums its frames in
+ * FP32 (registers or tensor memory) and adds that partial sum into d_acc once.
+ * CORRX_ACC_FP32 (the default): d_acc holds complex64, as the reference's row
+ * (corr-cuda/src/kernels.cu:252-264 accumulates complex64 across chunks).
+ * CORRX_ACC_FP64: d_acc holds complex128 (16 bytes per visibility), so a row
+ * summed over many launches keeps the precision of one launch; corrx_dump
+ * turns it into complex64. Applies to every later corrx_accumulate*,
+ * corrx_run_xengine, corrx_scale and batch created from the engine. The ABI
+ * contexts of corr_cuda.h always integrate in complex128 and hand back
+ * complex64 rows.
+ */
+#define CORRX_ACC_FP32 0
+#define CORRX_ACC_FP64 1
+corr_status corrx_set_accumulator(void *eng, int32_t precision);
+
+/* d_out (complex64, n_baseline*n_freq) = d_acc * (1/frames), rounded once from
+   the accumulator's precision; d_out may equal d_acc for an FP32 accumulator.
+   Both 16-byte aligned. */
+corr_status corrx_dump(void *eng, const void *d_acc, uint64_t frames, void *d_out,
+                       void *stream);
+
+/*
+ * Device ordinals of ABI contexts created after this call: configured device i
+ * (corr_config.devices[i], or device_id) runs on CUDA device physical[i]
+ * (i < n); n = 0 restores the identity. Process-wide. Meant for tests: several
+ * configured devices may share one GPU, each with its own buffers, streams and
+ * share of the work, so the multi-device paths (time slice, baseline range,
+ * pair covering) run on a one-GPU machine exactly as they would on several.
+ * No counterpart in the reference.
+ */
+corr_status corrx_set_device_map(const int32_t *physical, int32_t n);
+
+/*
+ * The placement corr_create would make for `cfg` on device index
+ * `device_index` (what corr_device_plan_get, corr_device_stations and
+ * corr_device_baselines report for it), computed on the host alone: no device
+ * is touched, so it works on a machine without a GPU. out_local receives, for
+ * each reported baseline, its index among the device's own baselines (j <= k
+ * over its stations, row-major). Any array may be NULL; a shorter array than
+ * the plan is CORR_ERR_ARG. Splits (CORR_SPLIT_*):
+ *   time slice     -- every device: every station, every baseline (a partial
+ *                     row over the slots with slot_seq % n_devices == index);
+ *   baseline range -- every device: every station, a contiguous range of
+ *                     n_baseline/n_devices baselines (+1 for the first
+ *                     n_baseline % n_devices devices);
+ *   pair covering  -- the stations are cut into m contiguous groups, m the
+ *                     largest with m(m-1)/2 <= n_devices; device d holds the
+ *                     d-th pair of groups (cyclically), and each baseline goes
+ *                     to the least-loaded device holding both its stations.
+ * No counterpart in the reference, whose planner runs inside corr_create.
+ */
+corr_status corrx_plan_query(const corr_config *cfg, int32_t device_index,
+                             corr_device_plan *out, int32_t *out_stations,
+                             int32_t stations_len, int32_t *out_baselines,
+                             int32_t baselines_len, int32_t *out_local, int32_t local_len);
 
 /* Synchronise the engine's device and report a tripped device watchdog
    (CORR_ERR_INTERNAL) or a CUDA error. */
@@ -203,18 +262,22 @@ corr_status corrx_batch_destroy(void *batch);
 
 /*
  * corrx_accumulate without any device allocation. No counterpart in the
- * reference. For callers that may not call cudaMalloc (a host that owns all
- * device memory through its own pool, code inside stream capture or a
- * real-time loop, a process with a fixed memory budget): the spectra between
- * the F- and X-engine live in a fixed 64 MiB device array inside the library
- * (held by every GPU that loads it until exit), so one call covers at most
- * 64 MiB / (n_station * n_freq * 8) frames -- 21 at 24 inputs and n_freq 16384;
- * more is rejected with CORR_ERR_ARG. Same arguments and result as
- * corrx_accumulate (d_acc += visibilities), plus the geometry and X-engine that
- * an engine would otherwise carry. The first call on a device looks up the
- * array's address with that device current: make it before any stream capture.
- * All calls share the array: calls whose kernels overlap on the GPU race, calls
- * ordered on one stream do not. Nothing in it needs to start at zero.
+ * reference. For callers that may not call cudaMalloc: a host that owns all
+ * device memory through its own pool and does not let libraries allocate, a
+ * real-time loop where an allocation (and the device synchronisation it can
+ * imply) would break a deadline, a process whose device-memory budget is fixed
+ * up front. The spectra between the F- and X-engine live in a fixed 64 MiB
+ * device array inside the library (held by every GPU that loads it until exit),
+ * so one call covers at most 64 MiB / (n_station * n_freq * e) frames, e = 4
+ * bytes per bin for CORR_X_TC_FP16 and 8 for the other forms (42 or 21 frames at
+ * 24 inputs and n_freq 16384); more is rejected with CORR_ERR_ARG before
+ * anything is launched. Same arguments and result as corrx_accumulate (d_acc +=
+ * visibilities, complex64), plus the geometry and X-engine that an engine would
+ * otherwise carry. The first call on a device sets that device up with it
+ * current (looks up the arrays' addresses and copies the twiddle tables of every
+ * transform length, synchronously): make it before any stream capture. All
+ * calls share the spectra array: calls whose kernels overlap on the GPU race,
+ * calls ordered on one stream do not. Nothing in it needs to start at zero.
  */
 corr_status corrx_accumulate_noalloc(int32_t n_station, int32_t n_freq, int32_t xmode,
                                      const int8_t *d_samples, size_t station_stride,

@@ -17,8 +17,12 @@ def drive_rows(pkg, x: np.ndarray, n_cum: int, frames_per_slot: int, mode: str =
                missing: np.ndarray | None = None, present: np.ndarray | None = None,
                xmode: int = 0, block_slots: int = 3, chunk_frames: int | None = None,
                rows_per_fetch: int | None = None, autotune: bool = False,
-               fplan: int | None = None):
+               fplan: int | None = None, devices: list[int] | None = None,
+               split_mode: int = 0, plans: list | None = None):
     """x: int8 [rows, n_station, n_cum, 2*n_freq] -> complex64 [rows, n_baseline, n_freq].
+
+    devices/split_mode: spread the context over several configured devices
+    (corr_config.devices); plans: list that receives each device's placement.
 
     missing: bool [rows, n_cum] frames handled per `mode` (golden.c's three
     preparations); present: bool [rows, n_station, n_cum] per-station validity
@@ -27,8 +31,11 @@ def drive_rows(pkg, x: np.ndarray, n_cum: int, frames_per_slot: int, mode: str =
     rows, n, _, L = x.shape
     nf = L // 2
     chunk = chunk_frames or min(frames_per_slot, 128)
-    cfg = pkg.make_config(n, nf, frames_per_slot, chunk, block_slots, rows_per_fetch or rows)
+    cfg = pkg.make_config(n, nf, frames_per_slot, chunk, block_slots, rows_per_fetch or rows,
+                          split_mode=split_mode, devices=devices)
     with pkg.Correlator(cfg) as c:
+        if plans is not None:   # what each device holds, as the context reports it
+            plans.extend(c.device_plan(d) for d in range(c.n_devices()))
         if xmode:
             c.set_xengine(xmode)
         if autotune:

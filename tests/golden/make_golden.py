@@ -14,14 +14,15 @@ and stores compact fixtures here:
     channel of every row and baseline plus float64 per-(row, baseline) sums over
     all channels, which keeps the fixture small.
 
-Usage: python tests/golden/make_golden.py [REFERENCE_ROOT]
-(REFERENCE_ROOT defaults to /root/reference). Only needed to regenerate the
-committed .npz files; the tests themselves never touch the reference.
+Usage: python tests/golden/make_golden.py REFERENCE_ROOT
+(or set CORR_REFERENCE_DIR). Only needed to regenerate the committed .npz
+files; the tests themselves never touch the reference.
 """
 
 from __future__ import annotations
 
 import hashlib
+import os
 import subprocess
 import sys
 import tempfile
@@ -46,7 +47,11 @@ def sha256(path: Path) -> str:
 
 
 def main() -> int:
-    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CORR_REFERENCE_DIR")
+    if not root:
+        print("usage: make_golden.py REFERENCE_ROOT (or set CORR_REFERENCE_DIR)", file=sys.stderr)
+        return 2
+    ref = Path(root)
     gen = ref / "corr-cuda" / "tests" / "gen_golden.py"
     if not gen.exists():
         print(f"{gen} not found", file=sys.stderr)

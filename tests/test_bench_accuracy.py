@@ -1,4 +1,5 @@
-"""bench.py's accuracy report (float64 DFT at a channel subset), on the CPU.
+"""bench.py's accuracy report (float64 DFT at a channel subset, and the float64
+FFT reference over the whole row), on the CPU.
 
 Rows from the float64 oracle must come out exact to single precision; rows
 with a planted error must show it; lost frames must be zeroed as the engines do.
@@ -32,6 +33,10 @@ def test_accuracy_report_against_the_oracle(oracle):
     assert rep["vs_fp64"]["plain"]["max_per_vis"] < 1e-6
     assert abs(rep["vs_fp64"]["tc"]["rel_rms"] - 1e-3) < 1e-5
     assert abs(rep["vs_plain"]["tc"]["rel_rms"] - 1e-3) < 1e-5
+    # every visibility of the row against the float64 FFT reference
+    assert rep["vs_fp64_full_row"]["plain"]["rel_rms"] < 1e-6
+    assert rep["vs_fp64_full_row"]["plain"]["max_per_vis"] < 1e-6
+    assert abs(rep["vs_fp64_full_row"]["tc"]["rel_rms"] - 1e-3) < 1e-5
 
 
 def test_accuracy_report_zeroes_lost_packets(oracle):

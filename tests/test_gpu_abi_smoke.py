@@ -122,7 +122,8 @@ def test_device_introspection(pkg, cuda):
         assert lib.corr_device_baselines(c.ctx, 0, bl, 10) == OK and list(bl) == list(range(10))
 
 
-def test_multi_device_config_is_refused_cleanly(pkg, cuda, lib):
+def test_multi_device_config_checks(pkg, cuda, lib):
+    """Repeated or invisible devices are refused; distinct visible ones are accepted."""
     cfg = smoke_config(pkg)
     n = cuda.cuda.device_count()
     cfg.n_devices = 2
@@ -132,7 +133,9 @@ def test_multi_device_config_is_refused_cleanly(pkg, cuda, lib):
     assert lib.corr_create(C.byref(cfg), C.byref(ctx)) == ARG
     if n >= 2:
         cfg.devices[1] = 1
-        assert lib.corr_create(C.byref(cfg), C.byref(ctx)) == 8   # NOT_IMPL
+        assert lib.corr_create(C.byref(cfg), C.byref(ctx)) == OK
+        assert lib.corr_n_devices(ctx) == 2
+        assert lib.corr_destroy(ctx) == OK
     cfg.n_devices = 1
     cfg.devices[0] = n   # out of range
     assert lib.corr_create(C.byref(cfg), C.byref(ctx)) == ARG

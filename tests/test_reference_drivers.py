@@ -10,8 +10,8 @@ matching declaration. abi_smoke then runs on the CPU: its device-free sections
 that need a visible GPU fail here exactly as they do for the reference library
 without one (cudaGetDeviceCount fails -> CORR_ERR_CUDA, corr_cuda.cpp:594-597).
 
-Skipped when the reference tree or gcc is absent (the reference sources are
-read in place, never copied).
+The reference checkout is named by CORR_REFERENCE_DIR; skipped when it is unset
+or gcc is absent (the reference sources are read in place, never copied).
 """
 
 from __future__ import annotations
@@ -23,13 +23,15 @@ from pathlib import Path
 
 import pytest
 
-REF = Path(os.environ.get("CORR_REFERENCE_DIR", "/root/reference")) / "corr-cuda" / "tests"
+_ROOT = os.environ.get("CORR_REFERENCE_DIR")   # the reference checkout, when present
+REF = Path(_ROOT) / "corr-cuda" / "tests" if _ROOT else None
 REPO = Path(__file__).resolve().parents[1]
 LIB = REPO / "21cma_abf_correlator_gb300" / "lib"
 DRIVERS = ["abi_smoke", "async_notify", "bench", "golden", "multi_device"]
 
-pytestmark = pytest.mark.skipif(not REF.is_dir() or shutil.which("gcc") is None,
-                                reason="reference C drivers or gcc not available")
+pytestmark = pytest.mark.skipif(REF is None or not REF.is_dir() or shutil.which("gcc") is None,
+                                reason="CORR_REFERENCE_DIR unset, or the reference's C drivers "
+                                       "or gcc not available")
 
 
 def build(name: str, out: Path) -> subprocess.CompletedProcess:

@@ -1,14 +1,18 @@
 """corrx_accumulate_noalloc: the allocation-free accumulate, checked against corrx_accumulate.
 
-Some callers of this library may not allocate device memory (their host owns
-every device byte through its own pool, or they run inside stream capture or a
-real-time loop where cudaMalloc is not allowed). For them the library keeps the
-spectra scratch in a fixed 64 MiB device array instead of a buffer that
-corrx_create allocates. This file checks, through the C ABI, that two calls in
-a row give the same visibilities as the allocating entry point (same kernels;
-tolerance 1e-5 relative RMS, the plain-path bar), that the second call is not
-disturbed by what the first left in the shared array, and that a request larger
-than the array is refused with CORR_ERR_ARG. It is collected last on purpose.
+Some callers of this library may not allocate device memory: their host owns
+every device byte through its own pool, or they run a real-time loop in which an
+allocation (and the device synchronisation it can bring) would break a
+deadline, or their device-memory budget is fixed up front. For them the library
+keeps the spectra scratch in a fixed 64 MiB device array instead of a buffer
+that corrx_create allocates, and the twiddle tables of every transform length in
+a second fixed array filled once per device. This file checks, through the C
+ABI, that two calls in a row give the same visibilities as the allocating entry
+point (same kernels; tolerance 1e-5 relative RMS, the plain-path bar), that the
+second call is not disturbed by what the first left in the shared array, that
+calls of different transform lengths follow each other correctly, that the FP16
+form holds twice the frames (4-byte bins), and that a request larger than the
+array is refused with CORR_ERR_ARG. It is collected last on purpose.
 """
 
 from __future__ import annotations
@@ -74,3 +78,41 @@ def test_request_beyond_the_array_is_refused(pkg, cuda):
     assert "21 frames" in msg and "split the call" in msg
     torch.cuda.synchronize()
     assert not torch.any(acc)               # nothing was launched
+
+
+def test_fp16_form_holds_twice_the_frames(pkg, cuda):
+    """FP16 spectra take 4 bytes a bin: 42 frames fit at 24 inputs, 43 do not."""
+    torch = cuda
+    n, nf = 24, 16384
+    rng = np.random.default_rng(7)
+    x = torch.from_numpy(rng.integers(-60, 61, size=(n, 43, 2 * nf)).astype(np.int8)).cuda()
+    acc = torch.zeros((n * (n + 1) // 2, nf), dtype=torch.complex64, device="cuda")
+    assert noalloc(pkg, torch, 1, x, 43, acc) == pkg.abi.CORR_ERR_ARG
+    assert "42 frames" in pkg.abi.load().corr_last_error().decode()
+    assert noalloc(pkg, torch, 1, x, 42, acc) == 0
+    eng = pkg.FxEngine(n, nf, max_frames=64, xmode=1)
+    want = eng.new_acc()
+    eng.accumulate(x, 42, want)
+    torch.cuda.synchronize()
+    eng.check()
+    assert np.array_equal(acc.cpu().numpy(), want.cpu().numpy())
+    eng.close()
+
+
+def test_calls_of_different_lengths_in_a_row(pkg, cuda):
+    """Each transform length reads its own twiddle tables: 4096, 16384 and 512
+    channels back to back on one stream, each equal to the allocating path."""
+    torch = cuda
+    rng = np.random.default_rng(11)
+    for nf in (4096, 16384, 512, 4096):
+        n, frames = 6, 16
+        x = torch.from_numpy(rng.integers(-60, 61, size=(n, frames, 2 * nf)).astype(np.int8)).cuda()
+        got = torch.zeros((n * (n + 1) // 2, nf), dtype=torch.complex64, device="cuda")
+        assert noalloc(pkg, torch, 0, x, frames, got) == 0
+        eng = pkg.FxEngine(n, nf, max_frames=frames)
+        want = eng.new_acc()
+        eng.accumulate(x, frames, want)
+        torch.cuda.synchronize()
+        eng.check()
+        assert np.array_equal(got.cpu().numpy(), want.cpu().numpy()), f"n_freq {nf}"
+        eng.close()
