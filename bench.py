@@ -42,7 +42,7 @@ REPO = Path(__file__).resolve().parent
 sys.path.insert(0, str(REPO))
 PKG_NAME = "21cma_abf_correlator_gb300"
 METRIC = "fused F+X GSample/s"
-PASS_FRAMES = 1024        # default frames per F/X pass on the device-resident path
+PASS_FRAMES = 2048        # default frames per F/X pass on the device-resident path
 
 
 def peaks():
