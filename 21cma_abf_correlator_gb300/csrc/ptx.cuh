@@ -94,6 +94,11 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32
         : "memory");
 }
 
+// *dst += v, performed at L2, with no value returned to the thread.
+__device__ __forceinline__ void red_add_f64(double *dst, double v) {
+    asm volatile("red.global.add.f64 [%0], %1;" ::"l"(gmem_addr(dst)), "d"(v) : "memory");
+}
+
 // 16-byte cp.async with zero fill when src_bytes == 0.
 __device__ __forceinline__ void cp_async16(void *dst, const void *src, uint32_t src_bytes) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(dst)),

@@ -721,33 +721,19 @@ __global__ void __launch_bounds__(kThreads, 1)
                 return static_cast<size_t>(b) * p.n_freq + c0 + c;
             };
             if (p.acc64) {
-                // complex128 row: the launch's FP32 sums are added in double
-                double2 *acc = static_cast<double2 *>(p.acc);
-                for (int q0 = et; q0 < n_items; q0 += kEpilogue * kBatch) {
-                    double2 a[kBatch][2];
-#pragma unroll
-                    for (int u = 0; u < kBatch; ++u) {
-                        const int q = q0 + u * kEpilogue;
-                        if (q < n_items) {
-                            const double2 *src = acc + row_offset(q);
-                            a[u][0] = src[0];
-                            a[u][1] = src[1];
-                        }
-                    }
-#pragma unroll
-                    for (int u = 0; u < kBatch; ++u) {
-                        const int q = q0 + u * kEpilogue;
-                        if (q >= n_items) break;
-                        float2 v0, v1;
-                        vis(q, v0, v1);
-                        a[u][0].x += v0.x;
-                        a[u][0].y += v0.y;
-                        a[u][1].x += v1.x;
-                        a[u][1].y += v1.y;
-                        double2 *dst = acc + row_offset(q);
-                        dst[0] = a[u][0];
-                        dst[1] = a[u][1];
-                    }
+                // complex128 row: the launch's FP32 sums are added in double, as
+                // reductions performed in L2 (red.global.add.f64): this CTA is the
+                // only writer of these values in the launch, so the result is the
+                // same as a read-modify-write, without waiting for the reads.
+                double *acc = static_cast<double *>(p.acc);
+                for (int q = et; q < n_items; q += kEpilogue) {
+                    float2 v0, v1;
+                    vis(q, v0, v1);
+                    double *dst = acc + 2 * row_offset(q);
+                    red_add_f64(dst + 0, v0.x);
+                    red_add_f64(dst + 1, v0.y);
+                    red_add_f64(dst + 2, v1.x);
+                    red_add_f64(dst + 3, v1.y);
                 }
             } else {
                 float2 *acc = static_cast<float2 *>(p.acc);

@@ -42,7 +42,7 @@ REPO = Path(__file__).resolve().parent
 sys.path.insert(0, str(REPO))
 PKG_NAME = "21cma_abf_correlator_gb300"
 METRIC = "fused F+X GSample/s"
-PASS_FRAMES = 2048        # default frames per F/X pass on the device-resident path
+PASS_FRAMES = 1024        # default frames per F/X pass on the device-resident path
 
 
 def peaks():
@@ -507,8 +507,11 @@ def main() -> None:
 
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
-        # the reference's CPU formulation on every host core, as the reference arm runs it
-        cpu = time_cpu_oracle(w, args.cpu_seconds, os.cpu_count() or 1)
+        # the reference's CPU formulation on every host core, as the reference arm
+        # runs it: one short warm-up round, then the measured one
+        procs = os.cpu_count() or 1
+        time_cpu_oracle(w, min(3.0, args.cpu_seconds), procs)
+        cpu = time_cpu_oracle(w, args.cpu_seconds, procs)
         cpu["kind"] = "port"
 
     passes = math.ceil(F / PASS_FRAMES)

@@ -16,8 +16,11 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("acc64", [False, True], ids=["fp32rows", "fp64rows"])
 @pytest.mark.parametrize("xmode", [0, 2])
-def test_batch_graph_rows_match_oracle(pkg, cuda, oracle, xmode):
+def test_batch_graph_rows_match_oracle(pkg, cuda, oracle, xmode, acc64):
+    """With complex128 accumulators (corrx_set_accumulator) each block integrates
+    in one FP64 row of the batch and is dumped, divided, into its complex64 row."""
     torch = cuda
     lib = pkg.abi.load()
     n, nf, pool = 6, 2048, 300
@@ -29,6 +32,8 @@ def test_batch_graph_rows_match_oracle(pkg, cuda, oracle, xmode):
     first = (C.c_int64 * len(blocks))(*[b[0] for b in blocks])
     frames = (C.c_int32 * len(blocks))(*[b[1] for b in blocks])
     eng = pkg.FxEngine(n, nf, max_frames=48, xmode=xmode)
+    if acc64:
+        eng.set_accumulator(pkg.abi.CORRX_ACC_FP64)
     xs = torch.from_numpy(x).cuda()
     ms = torch.from_numpy(mask).cuda()
     nb = n * (n + 1) // 2
