@@ -65,13 +65,18 @@ corr_status check_geometry(int n_station, int n_freq) {
                      "are supported",
                      n_station, n_station * (n_station + 1) / 2);
     if (n_freq < 1) return fail(CORR_ERR_ARG, "n_freq must be >= 1");
-    if (!is_pow2(n_freq) || n_freq < 512 || n_freq > 16384) {
+    // Powers of two from 512, and the reference's multiples of 2048 (frames of
+    // whole 4096-sample packets), up to 16384: the F-engine's transform lengths.
+    const bool pow2 = is_pow2(n_freq) && n_freq >= 512;
+    if ((!pow2 && n_freq % 2048 != 0) || n_freq > 16384) {
         if (n_freq % 2048 == 0)
             return failf(CORR_ERR_NOT_IMPL,
-                         "n_freq=%d: the F-engine transforms power-of-two frames only "
-                         "(n_freq in 512..16384)",
+                         "n_freq=%d: frames longer than 32768 samples (n_freq above 16384) "
+                         "are not supported",
                          n_freq);
-        return failf(CORR_ERR_ARG, "n_freq=%d is not a power of two in [512, 16384]", n_freq);
+        return failf(CORR_ERR_ARG,
+                     "n_freq=%d is neither a multiple of 2048 nor a power of two in [512, 16384]",
+                     n_freq);
     }
     return CORR_OK;
 }
@@ -405,8 +410,10 @@ corr_status fxplan_set_tiles(FxPlan *p, int ytile, int xct, int xkt, int fplan) 
     if (!fengine_plan_ok(p->n_freq, fplan, spectra_format(p->xmode)))
         return failf(CORR_ERR_ARG, "FFT plan %d does not write the spectra of X-engine mode %d",
                      fplan, p->xmode);
-    if (ytile < 2 || ytile > p->n_freq || (ytile & (ytile - 1)) != 0)
-        return failf(CORR_ERR_ARG, "ytile=%d is not a power of two in [2, n_freq=%d]", ytile,
+    if (ytile != p->n_freq &&
+        (ytile < 2 || (ytile & (ytile - 1)) != 0 || p->n_freq % ytile != 0))
+        return failf(CORR_ERR_ARG,
+                     "ytile=%d is neither n_freq=%d nor a power of two >= 2 dividing it", ytile,
                      p->n_freq);
     if (p->xmode != CORR_X_PLAIN_FP32) {
         if (!xengine_tc_shape_ok(p->n_station, p->xmode == CORR_X_TC_FP16_SPLIT, xct, xkt))

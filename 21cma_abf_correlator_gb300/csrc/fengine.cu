@@ -12,8 +12,9 @@
 //     as zeros, which is what zeroing the samples and transforming them gives;
 //   * the real frame x[0..L) (L = 2M) is packed as M complex points
 //     z[n] = x[2n] + i*x[2n+1] and transformed by a Stockham autosort FFT in
-//     shared memory (three or four passes of radix 8..32, FePlan below), FP32
-//     in registers, twiddles from host-computed double-precision tables;
+//     shared memory (three or four passes of radix 8..32, led by a radix-3, 5
+//     or 7 pass when M is not a power of two; FePlan below), FP32 in
+//     registers, twiddles from host-computed double-precision tables;
 //   * the split X[k] = Fe[k] + w^k Fo[k] turns Z into the L-point real spectrum;
 //     bins 0..M-1 are written, the Nyquist bin M is dropped and nothing is
 //     normalised (reference semantics, HANDOFF.md:583-602).
@@ -38,7 +39,8 @@ namespace {
 
 // ---------------------------------------------------------------------------
 // Small DFTs in registers, forward sign (exp(-2*pi*i*n*k/R)), natural order.
-// All constant twiddles are 32nd roots of unity.
+// The power-of-two radices' constant twiddles are 32nd roots of unity; the odd
+// radices 3, 5 and 7 (first pass of lengths 3, 5 or 7 x 2^k) use their own.
 // ---------------------------------------------------------------------------
 
 template <int R>
@@ -64,6 +66,61 @@ struct Dft<4> {
         v[3] = make_float2(d02.x - d13.y, d02.y + d13.x); // d02 + i*d13
     }
 };
+
+// cos(2*pi*m/R) and sin(2*pi*m/R) for the odd radices R = 3, 5, 7 and
+// m = 1..(R-1)/2 (the values of the circle functions at those angles, to 21 digits).
+__host__ __device__ constexpr float cos_odd(int R, int m) {
+    return R == 3 ? -0.5f
+         : R == 5 ? (m == 1 ? 0.309016994374947424102f : -0.809016994374947424102f)
+                  : (m == 1 ? 0.623489801858733530525f
+                   : m == 2 ? -0.222520933956314404289f
+                            : -0.900968867902419126236f);
+}
+__host__ __device__ constexpr float sin_odd(int R, int m) {
+    return R == 3 ? 0.866025403784438646764f
+         : R == 5 ? (m == 1 ? 0.951056516295153572116f : 0.587785252292473129169f)
+                  : (m == 1 ? 0.781831482468029808708f
+                   : m == 2 ? 0.974927912181823607018f
+                            : 0.433883739117558120476f);
+}
+
+// Odd R: the inputs n and R-n meet the same cosine and opposite sines, so with
+// s_n = x[n] + x[R-n] and d_n = x[n] - x[R-n] (n = 1..H, H = (R-1)/2)
+//   X[k]   = x[0] + sum_n s_n cos(2*pi*n*k/R) - i sum_n d_n sin(2*pi*n*k/R)
+//   X[R-k] = the same with +i,                     k = 1..H.
+template <int R>
+struct DftOdd {
+    static constexpr int H = (R - 1) / 2;
+    static __device__ __forceinline__ void run(float2 *v) {
+        float2 s[H], d[H];
+        float2 sum = v[0];
+#pragma unroll
+        for (int n = 1; n <= H; ++n) {
+            s[n - 1] = cadd(v[n], v[R - n]);
+            d[n - 1] = csub(v[n], v[R - n]);
+            sum = cadd(sum, s[n - 1]);
+        }
+        const float2 x0 = v[0];
+#pragma unroll
+        for (int k = 1; k <= H; ++k) {
+            float2 a = x0, b = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int n = 1; n <= H; ++n) {
+                const int m = (n * k) % R;   // angle 2*pi*m/R; beyond H the sine changes sign
+                const float c = cos_odd(R, m <= H ? m : R - m);
+                const float sn = m <= H ? sin_odd(R, m) : -sin_odd(R, R - m);
+                a = make_float2(fmaf(s[n - 1].x, c, a.x), fmaf(s[n - 1].y, c, a.y));
+                b = make_float2(fmaf(d[n - 1].x, sn, b.x), fmaf(d[n - 1].y, sn, b.y));
+            }
+            v[k] = make_float2(a.x + b.y, a.y - b.x);       // a - i*b
+            v[R - k] = make_float2(a.x - b.y, a.y + b.x);   // a + i*b
+        }
+        v[0] = sum;
+    }
+};
+template <> struct Dft<3> : DftOdd<3> {};
+template <> struct Dft<5> : DftOdd<5> {};
+template <> struct Dft<7> : DftOdd<7> {};
 
 // R = 4 x (R/4): n = (R/4)*n1 + n2, k = k1 + 4*k2.
 template <int R>
@@ -129,30 +186,38 @@ __device__ __forceinline__ void apply_twiddles(float2 *v, int u, const float2 *l
     for (int r = 1; r < R; ++r) v[r] = cmul(v[r], w[r]);
 }
 
-// Radix plan per transform length M = 2^LOGM: three passes R0 x R1 x R2 = M,
-// P = 2*R2 points per thread, T = M/P threads. The last pass (radix R2) is
-// fused with the real-FFT split: thread t owns butterflies t and J - t
-// (J = M/R2), so Z[k] and Z[M-k] meet in its registers. Plan 0 has three
-// passes (R0 x R1 x R2, R1b = 1); plan 1, where a size has one, has four
+// Radix plan per transform length M: three passes R0 x R1 x R2 = M, P = 2*R2
+// points per thread, T = M/P threads. The last pass (radix R2) is fused with
+// the real-FFT split: thread t owns butterflies t and J - t (J = M/R2), so Z[k]
+// and Z[M-k] meet in its registers. Plan 0 of a power of two has three passes
+// (R0 x R1 x R2, R1b = 1); plan 1, where a size has one, has four
 // (R0 x R1 x R1b x R2) with half the points per thread and twice the threads:
 // one more shared-memory pass against twice the warps to hide latency. The
-// autotuner times both.
-template <int LOGM, int PLAN>
+// autotuner times both. A length of 3, 5 or 7 x 2^k (the multiples of 2048 up
+// to 16384 that are not powers of two: a frame of whole 4096-sample packets)
+// starts with that odd radix, whose pass has no twiddles, then three
+// power-of-two passes.
+template <int M, int PLAN>
 struct FePlan;
-template <> struct FePlan<14, 0> { static constexpr int R0 = 32, R1 = 32, R1b = 1, R2 = 16; };
-template <> struct FePlan<14, 1> { static constexpr int R0 = 16, R1 = 16, R1b = 8, R2 = 8; };
-template <> struct FePlan<13, 0> { static constexpr int R0 = 32, R1 = 16, R1b = 1, R2 = 16; };
-template <> struct FePlan<12, 0> { static constexpr int R0 = 16, R1 = 16, R1b = 1, R2 = 16; };
-template <> struct FePlan<11, 0> { static constexpr int R0 = 16, R1 = 8, R1b = 1, R2 = 16; };
-template <> struct FePlan<10, 0> { static constexpr int R0 = 16, R1 = 8, R1b = 1, R2 = 8; };
-template <> struct FePlan<9, 0> { static constexpr int R0 = 16, R1 = 4, R1b = 1, R2 = 8; };
+template <> struct FePlan<16384, 0> { static constexpr int R0 = 32, R1 = 32, R1b = 1, R2 = 16; };
+template <> struct FePlan<16384, 1> { static constexpr int R0 = 16, R1 = 16, R1b = 8, R2 = 8; };
+template <> struct FePlan<14336, 0> { static constexpr int R0 = 7, R1 = 16, R1b = 8, R2 = 16; };
+template <> struct FePlan<12288, 0> { static constexpr int R0 = 3, R1 = 32, R1b = 8, R2 = 16; };
+template <> struct FePlan<10240, 0> { static constexpr int R0 = 5, R1 = 16, R1b = 8, R2 = 16; };
+template <> struct FePlan<8192, 0> { static constexpr int R0 = 32, R1 = 16, R1b = 1, R2 = 16; };
+template <> struct FePlan<6144, 0> { static constexpr int R0 = 3, R1 = 16, R1b = 8, R2 = 16; };
+template <> struct FePlan<4096, 0> { static constexpr int R0 = 16, R1 = 16, R1b = 1, R2 = 16; };
+template <> struct FePlan<2048, 0> { static constexpr int R0 = 16, R1 = 8, R1b = 1, R2 = 16; };
+template <> struct FePlan<1024, 0> { static constexpr int R0 = 16, R1 = 8, R1b = 1, R2 = 8; };
+template <> struct FePlan<512, 0> { static constexpr int R0 = 16, R1 = 4, R1b = 1, R2 = 8; };
 
-template <int LOGM, int PLAN>
+template <int MM, int PLAN>
 struct FeCfg {
-    using Plan = FePlan<LOGM, PLAN>;
-    static constexpr int M = 1 << LOGM;
+    using Plan = FePlan<MM, PLAN>;
+    static constexpr int M = MM;
     static constexpr int R0 = Plan::R0, R1 = Plan::R1, R1b = Plan::R1b, R2 = Plan::R2;
     static_assert(R0 * R1 * R1b * R2 == M, "radix plan must cover M");
+    static_assert(M % 64 == 0, "the two-level twiddle tables step by 64");
     static constexpr int P = 2 * R2;                // points per thread
     static constexpr int T = M / P;                 // threads per CTA
     static constexpr int J = M / R2;                // butterflies of the last pass
@@ -196,30 +261,47 @@ __device__ __forceinline__ float2 int8_pair_to_float2(uint16_t u) {
 template <int SHIFT>
 __device__ __forceinline__ int padi(int i) { return i + (i >> SHIFT); }
 
+// j / D and j % D for a compile-time D and j >= 0: a shift and a mask for a
+// power of two, a multiply-high otherwise.
+template <int D>
+__device__ __forceinline__ int div_c(int j) {
+    return static_cast<int>(static_cast<unsigned>(j) / static_cast<unsigned>(D));
+}
+template <int D>
+__device__ __forceinline__ int mod_c(int j) {
+    return static_cast<int>(static_cast<unsigned>(j) % static_cast<unsigned>(D));
+}
+
 // Stockham pass of radix R over M points with sub-transform size NS:
 //   out[(j/NS)*NS*R + j%NS + r*NS] = DFT_R( in[j + r*M/R] * w^(r*(j%NS)) )
-// Each thread owns P/R butterflies. In place: read all, barrier, write all,
-// barrier. The first pass reads int8 sample pairs instead of shared data.
-// TAB: the pass's twiddles w^(r*(j%NS)) (NS*R of them) come from table `t2`
-// laid out [r][j%NS] instead of from the two-level tables.
+// for the M/R butterflies j. Each thread owns ceil(P/R) of them (j = tid + q*T);
+// where R does not divide P (an odd first radix) the last round of butterflies
+// is partial and the threads past M/R sit it out. In place: read all, barrier,
+// write all, barrier. The first pass reads int8 sample pairs instead of shared
+// data. TAB: the pass's twiddles w^(r*(j%NS)) (NS*R of them) come from table
+// `t2` laid out [r][j%NS] instead of from the two-level tables.
 template <int M, int T, int P, int R, int NS, int SHIFT, bool FIRST, bool TAB = false>
 __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *__restrict__ sx,
                                          const float2 *lo, const float2 *hi, int tid,
                                          const float2 *t2 = nullptr) {
-    constexpr int NB = P / R;
+    constexpr int NB = (P + R - 1) / R;
     constexpr int STRIDE = M / R;
-    static_assert(NB >= 1 && NB * R == P, "bad radix plan");
-    // Every index below is a padded per-thread base plus a compile-time offset:
-    // the read stride and the write stride are multiples of the padding period
-    // (or, for the first pass, offsets stay inside one period).
+    constexpr bool EXACT = NB * R == P;   // NB*T == M/R: every thread has NB butterflies
+    static_assert(M % (NS * R) == 0, "bad radix plan");
+    // Reads: a padded per-thread base plus a compile-time offset, since the read
+    // stride is a multiple of the padding period. Writes likewise when the write
+    // stride NS is (or, in a first pass of radix 2^SHIFT, stays inside one
+    // period); otherwise (odd radices, and the pass after an odd first one) each
+    // element's padded index is computed on its own.
     static_assert(STRIDE % (1 << SHIFT) == 0, "read stride");
-    static_assert(NS % (1 << SHIFT) == 0 || (NS == 1 && R == (1 << SHIFT)), "write stride");
+    constexpr bool RUNS = NS % (1 << SHIFT) == 0 || (NS == 1 && R == (1 << SHIFT));
     constexpr int PSTRIDE = STRIDE + (STRIDE >> SHIFT);
     constexpr int PNS = (NS == 1) ? 1 : NS + (NS >> SHIFT);
     float2 v[NB][R];
 #pragma unroll
     for (int q = 0; q < NB; ++q) {
         const int j = tid + q * T;
+        if (!EXACT && j >= STRIDE) continue;
         if constexpr (FIRST) {
 #pragma unroll
             for (int r = 0; r < R; ++r)
@@ -231,11 +313,11 @@ __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *_
             for (int r = 0; r < R; ++r) v[q][r] = sd[pj + r * PSTRIDE];
         }
         if constexpr (TAB) {
-            const float2 *tj = t2 + (j & (NS - 1));
+            const float2 *tj = t2 + mod_c<NS>(j);
 #pragma unroll
             for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], tj[r * NS]);
         } else if constexpr (NS > 1) {
-            apply_twiddles<R>(v[q], (j & (NS - 1)) * (M / (NS * R)), lo, hi);
+            apply_twiddles<R>(v[q], mod_c<NS>(j) * (M / (NS * R)), lo, hi);
         }
         Dft<R>::run(v[q]);
     }
@@ -243,9 +325,16 @@ __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *_
 #pragma unroll
     for (int q = 0; q < NB; ++q) {
         const int j = tid + q * T;
-        const int pb = padi<SHIFT>((j & ~(NS - 1)) * R + (j & (NS - 1)));
+        if (!EXACT && j >= STRIDE) continue;
+        const int base = div_c<NS>(j) * (NS * R) + mod_c<NS>(j);
+        if constexpr (RUNS) {
+            const int pb = padi<SHIFT>(base);
 #pragma unroll
-        for (int r = 0; r < R; ++r) sd[pb + r * PNS] = v[q][r];
+            for (int r = 0; r < R; ++r) sd[pb + r * PNS] = v[q][r];
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) sd[padi<SHIFT>(base + r * NS)] = v[q][r];
+        }
     }
     __syncthreads();
 }
@@ -258,12 +347,12 @@ __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *_
 // warp diverges; only X[M/2] = conj(Z[M/2]) is one extra store for thread 0.
 // Split twiddles: k = j + i*J gives w_k = w_j * exp(-pi*i*i/R2), one table
 // lookup per butterfly times compile-time constants.
-template <int LOGM, int PLAN, class Row>
+template <int MM, int PLAN, class Row>
 __device__ __forceinline__ void last_pass_store(const float2 *__restrict__ sd,
                                                 const float2 *plo, const float2 *phi,
                                                 const float2 *qlo, const float2 *qhi,
                                                 const Row &yrow, int tid) {
-    using C = FeCfg<LOGM, PLAN>;
+    using C = FeCfg<MM, PLAN>;
     constexpr int M = C::M, J = C::J, R = C::R2, H = R / 2;
     static_assert(J % (1 << C::PADSHIFT) == 0, "last-pass stride");
     constexpr int PJ = J + (J >> C::PADSHIFT);
@@ -310,10 +399,10 @@ struct TwPtrs {
     const float2 *pass_lo, *pass_hi, *post_lo, *post_hi;
 };
 
-template <int LOGM, int PLAN, int FMT, bool CONTIG>
-__global__ void __launch_bounds__(FeCfg<LOGM, PLAN>::T, FeCfg<LOGM, PLAN>::MIN_BLOCKS)
+template <int MM, int PLAN, int FMT, bool CONTIG>
+__global__ void __launch_bounds__(FeCfg<MM, PLAN>::T, FeCfg<MM, PLAN>::MIN_BLOCKS)
     fengine_kernel(FengineArgs a, TwPtrs tw) {
-    using C = FeCfg<LOGM, PLAN>;
+    using C = FeCfg<MM, PLAN>;
     constexpr int M = C::M;
     constexpr int T = C::T;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -339,9 +428,10 @@ __global__ void __launch_bounds__(FeCfg<LOGM, PLAN>::T, FeCfg<LOGM, PLAN>::MIN_B
     for (int i = tid; i < C::N_PASS_HI; i += T) phi[i] = tw.pass_hi[i];
     for (int i = tid; i < C::N_POST_HI; i += T) qhi[i] = tw.post_hi[i];
     // second pass: t2[r][jj] = exp(-2*pi*i*r*jj/(R0*R1)) = w^u, u = r*jj*M/(R0*R1)
+    // (< M, as r < R1 and jj < R0)
     for (int i = tid; i < C::R0 * C::R1; i += T) {
         const int r = i / C::R0, jj = i - r * C::R0;
-        const int u = (r * jj * (M / (C::R0 * C::R1))) & (M - 1);
+        const int u = r * jj * (M / (C::R0 * C::R1));
         t2[i] = cmul(tw.pass_lo[u & 63], tw.pass_hi[u >> 6]);
     }
     if (tid == 0) {
@@ -434,27 +524,27 @@ __global__ void __launch_bounds__(FeCfg<LOGM, PLAN>::T, FeCfg<LOGM, PLAN>::MIN_B
         if constexpr (C::R1b > 1)
             fft_pass<M, T, C::P, C::R1b, C::R0 * C::R1, C::PADSHIFT, false>(sd, nullptr, plo, phi,
                                                                           tid);
-        last_pass_store<LOGM, PLAN>(sd, plo, phi, qlo, qhi, yrow, tid);
+        last_pass_store<MM, PLAN>(sd, plo, phi, qlo, qhi, yrow, tid);
         // The next item's first pass synchronises before it overwrites sd.
     }
 }
 
-template <int LOGM, int PLAN, int FMT, bool CONTIG>
+template <int MM, int PLAN, int FMT, bool CONTIG>
 corr_status launch_one(const FengineArgs &a, const TwiddleTables &tw, int num_sms,
                        cudaStream_t stream) {
-    using C = FeCfg<LOGM, PLAN>;
+    using C = FeCfg<MM, PLAN>;
     // Shared-memory limit and residency are per device: set up once on each.
     static PerDevice setup;
     static int per_sm[kMaxDeviceOrdinals];
     corr_status st = setup.run([](int dev) {
         corr_status s2 = cuda_check(
-            cudaFuncSetAttribute(fengine_kernel<LOGM, PLAN, FMT, CONTIG>,
+            cudaFuncSetAttribute(fengine_kernel<MM, PLAN, FMT, CONTIG>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM),
             "cudaFuncSetAttribute(fengine)");
         if (s2 != CORR_OK) return s2;
         int blocks = 0;
         s2 = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                            &blocks, fengine_kernel<LOGM, PLAN, FMT, CONTIG>, C::T, C::SMEM),
+                            &blocks, fengine_kernel<MM, PLAN, FMT, CONTIG>, C::T, C::SMEM),
                         "cudaOccupancyMaxActiveBlocksPerMultiprocessor(fengine)");
         if (s2 != CORR_OK) return s2;
         if (blocks < 1)
@@ -470,40 +560,34 @@ corr_status launch_one(const FengineArgs &a, const TwiddleTables &tw, int num_sm
     int grid = num_sms * per_sm[dev];
     if (grid > items) grid = items;
     TwPtrs p{tw.pass_lo, tw.pass_hi, tw.post_lo, tw.post_hi};
-    fengine_kernel<LOGM, PLAN, FMT, CONTIG><<<grid, C::T, C::SMEM, stream>>>(a, p);
+    fengine_kernel<MM, PLAN, FMT, CONTIG><<<grid, C::T, C::SMEM, stream>>>(a, p);
     return cuda_check(cudaGetLastError(), "fengine_kernel launch");
 }
 
-template <int LOGM, int PLAN>
+template <int MM, int PLAN>
 corr_status launch_plan(const FengineArgs &a, const TwiddleTables &tw, int num_sms,
                         cudaStream_t stream) {
-    const bool contig = a.ytile == (1 << LOGM);
+    const bool contig = a.ytile == MM;
     if (a.y_fmt == kSpectraF16)
-        return contig ? launch_one<LOGM, PLAN, kSpectraF16, true>(a, tw, num_sms, stream)
-                      : launch_one<LOGM, PLAN, kSpectraF16, false>(a, tw, num_sms, stream);
+        return contig ? launch_one<MM, PLAN, kSpectraF16, true>(a, tw, num_sms, stream)
+                      : launch_one<MM, PLAN, kSpectraF16, false>(a, tw, num_sms, stream);
     if (a.y_fmt == kSpectraF16Split)
-        return contig ? launch_one<LOGM, PLAN, kSpectraF16Split, true>(a, tw, num_sms, stream)
-                      : launch_one<LOGM, PLAN, kSpectraF16Split, false>(a, tw, num_sms, stream);
-    if (contig) return launch_one<LOGM, PLAN, kSpectraF32, true>(a, tw, num_sms, stream);
-    return launch_one<LOGM, PLAN, kSpectraF32, false>(a, tw, num_sms, stream);
+        return contig ? launch_one<MM, PLAN, kSpectraF16Split, true>(a, tw, num_sms, stream)
+                      : launch_one<MM, PLAN, kSpectraF16Split, false>(a, tw, num_sms, stream);
+    if (contig) return launch_one<MM, PLAN, kSpectraF32, true>(a, tw, num_sms, stream);
+    return launch_one<MM, PLAN, kSpectraF32, false>(a, tw, num_sms, stream);
 }
 
-template <int LOGM>
+template <int MM>
 corr_status launch_size(const FengineArgs &a, const TwiddleTables &tw, int num_sms,
                         cudaStream_t stream) {
-    if constexpr (LOGM == 14) {
-        if (a.fplan == 1) return launch_plan<LOGM, 1>(a, tw, num_sms, stream);
+    if constexpr (MM == 16384) {
+        if (a.fplan == 1) return launch_plan<MM, 1>(a, tw, num_sms, stream);
         if (a.fplan == 2) return fengine_tc_launch(a, tw.tc_image, num_sms, stream);
     }
     if (a.fplan != 0)
-        return failf(CORR_ERR_ARG, "FFT plan %d is not available at n_freq=%d", a.fplan, 1 << LOGM);
-    return launch_plan<LOGM, 0>(a, tw, num_sms, stream);
-}
-
-int ilog2(int v) {
-    int l = 0;
-    while ((1 << l) < v) ++l;
-    return l;
+        return failf(CORR_ERR_ARG, "FFT plan %d is not available at n_freq=%d", a.fplan, MM);
+    return launch_plan<MM, 0>(a, tw, num_sms, stream);
 }
 
 } // namespace
@@ -567,15 +651,21 @@ void fengine_release(TwiddleTables *tw) {
 
 corr_status fengine_launch(int n_freq, const TwiddleTables &tw, const FengineArgs &a,
                            int num_sms, cudaStream_t stream) {
-    switch (ilog2(n_freq)) {
-    case 9: return launch_size<9>(a, tw, num_sms, stream);
-    case 10: return launch_size<10>(a, tw, num_sms, stream);
-    case 11: return launch_size<11>(a, tw, num_sms, stream);
-    case 12: return launch_size<12>(a, tw, num_sms, stream);
-    case 13: return launch_size<13>(a, tw, num_sms, stream);
-    case 14: return launch_size<14>(a, tw, num_sms, stream);
+    switch (n_freq) {
+    case 512: return launch_size<512>(a, tw, num_sms, stream);
+    case 1024: return launch_size<1024>(a, tw, num_sms, stream);
+    case 2048: return launch_size<2048>(a, tw, num_sms, stream);
+    case 4096: return launch_size<4096>(a, tw, num_sms, stream);
+    case 6144: return launch_size<6144>(a, tw, num_sms, stream);
+    case 8192: return launch_size<8192>(a, tw, num_sms, stream);
+    case 10240: return launch_size<10240>(a, tw, num_sms, stream);
+    case 12288: return launch_size<12288>(a, tw, num_sms, stream);
+    case 14336: return launch_size<14336>(a, tw, num_sms, stream);
+    case 16384: return launch_size<16384>(a, tw, num_sms, stream);
     default:
-        return failf(CORR_ERR_ARG, "F-engine: n_freq=%d is not a power of two in [512, 16384]",
+        return failf(CORR_ERR_ARG,
+                     "F-engine: n_freq=%d is neither a power of two in [512, 16384] nor a "
+                     "multiple of 2048 up to 16384",
                      n_freq);
     }
 }

@@ -11,7 +11,7 @@
 // transform length live in a second fixed array.
 //
 // Properties a caller must know:
-//   * scratch: kNoAllocScratchBytes (64 MiB) of spectra plus 14 KB of twiddle
+//   * scratch: kNoAllocScratchBytes (64 MiB) of spectra plus 28 KB of twiddle
 //     tables, held by every GPU that loads the library until the process exits;
 //   * one call may cover at most 64 MiB / (n_station * n_freq * e) frames, e the
 //     bytes a spectrum bin takes between the engines (4 for the FP16 tensor
@@ -39,13 +39,15 @@ namespace corrgb {
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;
-constexpr int kMinLogFreq = 9, kMaxLogFreq = 14;   // n_freq 512 .. 16384
+// The transform lengths the F-engine takes, each with its tables in the array.
+constexpr int kSizes[] = {512, 1024, 2048, 4096, 6144, 8192, 10240, 12288, 14336, 16384};
+constexpr int kNumSizes = static_cast<int>(sizeof(kSizes) / sizeof(kSizes[0]));
 
-// Offset of the twiddle tables of 2^l channels in the twiddle array.
-constexpr int twiddle_offset(int l) {
-    return l == kMinLogFreq ? 0 : twiddle_offset(l - 1) + twiddle_entries(1 << (l - 1));
+// Offset of the twiddle tables of kSizes[i] channels in the twiddle array.
+constexpr int twiddle_offset(int i) {
+    return i == 0 ? 0 : twiddle_offset(i - 1) + twiddle_entries(kSizes[i - 1]);
 }
-constexpr int kTwEntries = twiddle_offset(kMaxLogFreq + 1);
+constexpr int kTwEntries = twiddle_offset(kNumSizes);
 
 static __device__ __align__(256) float2 g_noalloc_spectra[kNoAllocScratchBytes / sizeof(float2)];
 static __device__ __align__(256) float2 g_noalloc_twiddles[kTwEntries];
@@ -78,8 +80,8 @@ corr_status scratch_for(int dev, DeviceScratch *out) {
         if (st != CORR_OK) return st;
         d.twiddles = static_cast<float2 *>(p);
         std::vector<float2> all, tab;
-        for (int l = kMinLogFreq; l <= kMaxLogFreq; ++l) {
-            fengine_twiddles_host(1 << l, &tab);
+        for (int i = 0; i < kNumSizes; ++i) {
+            fengine_twiddles_host(kSizes[i], &tab);
             all.insert(all.end(), tab.begin(), tab.end());
         }
         st = cuda_check(cudaMemcpy(d.twiddles, all.data(), all.size() * sizeof(float2),
@@ -133,10 +135,12 @@ extern "C" corr_status corrx_accumulate_noalloc(int32_t n_station, int32_t n_fre
     if ((st = scratch_for(dev, &d)) != CORR_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
-    int l = 0;
-    while ((1 << l) < n_freq) ++l;
+    int size_index = 0;
+    while (size_index < kNumSizes && kSizes[size_index] != n_freq) ++size_index;
+    if (size_index == kNumSizes)
+        return failf(CORR_ERR_INTERNAL, "no twiddle tables for n_freq=%d", n_freq);
     TwiddleTables tw;
-    twiddle_views(d.twiddles + twiddle_offset(l), n_freq, &tw);
+    twiddle_views(d.twiddles + twiddle_offset(size_index), n_freq, &tw);
 
     FengineArgs fa{};
     fa.samples = d_samples;

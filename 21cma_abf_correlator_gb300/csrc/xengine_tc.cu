@@ -413,7 +413,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                     mbar_arrive_expect_tx(&bars.load_full[slot],
                                           static_cast<uint32_t>(g.ld_stage));
                     // frames past `frames` (the map's last frame) arrive as zeros
-                    tma_load_4d(ld_ring + slot * g.ld_stage, &ymap, c0 & (p.ytile - 1), 0,
+                    tma_load_4d(ld_ring + slot * g.ld_stage, &ymap, c0 % p.ytile, 0,
                                 st * g.kt, c0 / p.ytile, &bars.load_full[slot]);
                 }
                 ++s_ld_issued;

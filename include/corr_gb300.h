@@ -35,7 +35,7 @@ corr_status corr_set_xengine(void *ctx, int32_t mode);
 typedef struct corrx_params {
     uint32_t struct_size; /* sizeof(corrx_params)                                 */
     int32_t  n_station;   /* 1..44                                                */
-    int32_t  n_freq;      /* power of two in [512, 16384]                         */
+    int32_t  n_freq;      /* 512, 1024, or a multiple of 2048 up to 16384          */
     int32_t  max_frames;  /* frames per F/X pass; sizes the spectra buffer
                              (max_frames*n_station*n_freq*8 bytes)               */
     int32_t  xmode;       /* CORR_X_*                                             */
@@ -161,7 +161,8 @@ typedef struct corrx_tiles {
     int32_t  ytile;
     int32_t  xct;
     int32_t  xkt;
-    int32_t  fplan;       /* F-engine FFT plan: 0 (three passes), or at n_freq
+    int32_t  fplan;       /* F-engine FFT plan: 0 (three passes; four at the
+                             lengths that are not powers of two), or at n_freq
                              16384 also 1 (four passes, twice the threads) and,
                              with FP16 spectra (CORR_X_TC_FP16) only, 2 (the
                              DFT stages as tcgen05 matrix products; faster, with

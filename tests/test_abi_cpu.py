@@ -153,7 +153,8 @@ def _cfg(pkg, **kw):
     (dict(abi_version=8), 2),              # CORR_ERR_ABI
     (dict(struct_size=72), 2),
     (dict(n_freq=4096 + 1024), 1),         # not a power of two / multiple of 2048
-    (dict(n_freq=6144), 8),                # multiple of 2048, not a power of two: NOT_IMPL
+    (dict(n_freq=18432), 8),               # multiple of 2048 above 16384: NOT_IMPL
+    (dict(n_freq=3072), 1),                # neither a power of two nor a multiple of 2048
     (dict(n_freq=256), 1),
     (dict(n_freq=32768), 8),
     (dict(block_slots=1), 1),

@@ -85,6 +85,27 @@ def test_plain_layouts_are_bit_identical(pkg, cuda, oracle, ytile):
     assert oracle.rel_rms(got, oracle.correlate(x, present)) < 1e-5
 
 
+@pytest.mark.parametrize("xmode,ytile", [(0, 32), (0, 2048), (1, 8), (2, 4)])
+def test_layouts_at_a_length_that_is_not_a_power_of_two(pkg, cuda, oracle, xmode, ytile):
+    """n_freq 10240 = 5 x 2048: channel tiles of a power of two that divides it
+    give the same bits as contiguous rows (plain form: any such width; tensor
+    forms: their own tile width)."""
+    n, nf, frames = 6, 10240, 24
+    x, present, mask = _case(n, nf, frames, 10)
+    base = _run(pkg, cuda, x, mask, xmode, None)
+    if xmode:
+        eng = pkg.FxEngine(n, nf, max_frames=32, xmode=xmode)
+        t = eng.tiles()
+        eng.close()
+        tiles = (ytile, ytile, t["xkt"])
+    else:
+        tiles = (ytile, 0, 0)
+    got = _run(pkg, cuda, x, mask, xmode, tiles)
+    assert np.array_equal(got, base)
+    bar = tol(xmode, frames)["rms"] if xmode else 1e-5
+    assert oracle.rel_rms(got, oracle.correlate(x, present)) < bar
+
+
 def test_bad_tiles_are_refused(pkg, cuda):
     eng = pkg.FxEngine(24, 1024, max_frames=16, xmode=2)
     try:
@@ -149,6 +170,14 @@ def test_unknown_fft_plan_is_refused(pkg, cuda):
         t = eng.tiles()
         with pytest.raises(pkg.abi.CorrError):
             eng.set_tiles(t["ytile"], t["xct"], t["xkt"], 1)   # n_freq 1024 has one plan
+        e2 = pkg.FxEngine(4, 12288, max_frames=8, xmode=1)   # one plan too
+        try:
+            t2 = e2.tiles()
+            for bad in (1, 2):
+                with pytest.raises(pkg.abi.CorrError):
+                    e2.set_tiles(t2["ytile"], t2["xct"], t2["xkt"], bad)
+        finally:
+            e2.close()
         with pytest.raises(pkg.abi.CorrError):
             eng.set_tiles(t["ytile"], t["xct"], t["xkt"], -1)
     finally:

@@ -83,9 +83,11 @@ def test_chunk_and_slot_boundaries_do_not_matter(pkg, cuda, oracle, synth):
 
 
 @pytest.mark.parametrize("xmode", [0, 1, 2])
-@pytest.mark.parametrize("n_freq", [512, 1024, 2048, 4096, 8192, 16384])
+@pytest.mark.parametrize("n_freq", [512, 1024, 2048, 4096, 6144, 8192, 10240, 12288, 14336,
+                                    16384])
 def test_every_transform_length(pkg, cuda, oracle, n_freq, xmode):
-    """Every F-engine size, writing each spectra format (FP32, FP16, FP16 hi/lo)."""
+    """Every F-engine size, writing each spectra format (FP32, FP16, FP16 hi/lo):
+    the powers of two and the multiples of 2048 that are 3, 5 or 7 x 2^k."""
     torch = cuda
     rng = np.random.default_rng(n_freq)
     n, frames = 3, 5
@@ -101,6 +103,25 @@ def test_every_transform_length(pkg, cuda, oracle, n_freq, xmode):
     tol = {0: PER_VIS_TOL, 2: 2e-5, 1: 6e-3 / np.sqrt(frames)}[xmode]
     assert oracle.normalized_max_err(got, ref, n) < tol
     eng.close()
+
+
+@pytest.mark.parametrize("n_freq", [6144, 10240, 12288, 14336])
+def test_abi_at_multiples_of_2048(pkg, cuda, oracle, n_freq):
+    """The reference takes any multiple of 2048 (corr-cuda/src/corr_cuda.cpp:501-509):
+    rows through the C ABI at the lengths that are not powers of two, with
+    missing frames, in the plain form and both tensor forms."""
+    rng = np.random.default_rng(n_freq + 1)
+    n, n_cum, fps = 5, 48, 16
+    x = rng.integers(-40, 41, size=(2, n, n_cum, 2 * n_freq)).astype(np.int8)
+    present = np.ones((2, n, n_cum), dtype=bool)
+    present[0, 1, 7] = present[1, 4, 40] = present[1, 0, 0] = False
+    ref = oracle.correlate_rows(x, n_cum, present)
+    for xmode, tol in ((0, REL_RMS_TOL), (2, 2e-5), (1, 1.5e-3 / np.sqrt(n_cum))):
+        got = drive_rows(pkg, x, n_cum, fps, present=present, chunk_frames=8, block_slots=3,
+                         rows_per_fetch=2, xmode=xmode)
+        assert oracle.rel_rms(got, ref) < tol, (n_freq, xmode)
+        if xmode == 0:
+            assert oracle.normalized_max_err(got, ref, n) < PER_VIS_TOL
 
 
 def test_extreme_samples(pkg, cuda, oracle):
