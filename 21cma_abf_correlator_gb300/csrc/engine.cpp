@@ -66,16 +66,16 @@ corr_status check_geometry(int n_station, int n_freq) {
                      n_station, n_station * (n_station + 1) / 2);
     if (n_freq < 1) return fail(CORR_ERR_ARG, "n_freq must be >= 1");
     // Powers of two from 512, and the reference's multiples of 2048 (frames of
-    // whole 4096-sample packets), up to 16384: the F-engine's transform lengths.
+    // whole 4096-sample packets), up to 32768: the F-engine's transform lengths.
     const bool pow2 = is_pow2(n_freq) && n_freq >= 512;
-    if ((!pow2 && n_freq % 2048 != 0) || n_freq > 16384) {
+    if ((!pow2 && n_freq % 2048 != 0) || n_freq > 32768) {
         if (n_freq % 2048 == 0)
             return failf(CORR_ERR_NOT_IMPL,
-                         "n_freq=%d: frames longer than 32768 samples (n_freq above 16384) "
+                         "n_freq=%d: frames longer than 65536 samples (n_freq above 32768) "
                          "are not supported",
                          n_freq);
         return failf(CORR_ERR_ARG,
-                     "n_freq=%d is neither a multiple of 2048 nor a power of two in [512, 16384]",
+                     "n_freq=%d is neither a multiple of 2048 nor a power of two in [512, 32768]",
                      n_freq);
     }
     return CORR_OK;

@@ -87,6 +87,9 @@ struct TwiddleTables {
     float2 *post_hi = nullptr;
     int n_pass_hi = 0;
     int n_post_hi = 0;
+    // n_freq above 16384 (two half-length transforms, M = n_freq/2 above):
+    // exp(-pi*i/n_freq), the odd bins' offset in the real-FFT split twiddle
+    float2 *odd_shift = nullptr;
     void *tc_image = nullptr;   // tensor-core FFT tables (plan 2, n_freq 16384)
 };
 
@@ -167,10 +170,17 @@ struct XengineArgs {
 };
 
 // fengine.cu
-/// Entries of the four twiddle tables for n_freq (pass_lo, pass_hi, post_lo, post_hi).
+/// Length of the F-engine's complex FFT for n_freq: n_freq itself up to 16384
+/// (one CTA's shared memory holds the frame); above that a frame is split by
+/// one radix-2 step into two sequences of n_freq/2 points, transformed one
+/// after the other by the same CTA (even bins, then odd bins).
+constexpr int fft_length(int n_freq) { return n_freq > 16384 ? n_freq / 2 : n_freq; }
+/// Entries reserved for n_freq's twiddle tables: the four tables of
+/// M = fft_length(n_freq) (pass_lo, pass_hi, post_lo, post_hi), then, for the
+/// split lengths, odd_shift; zero-padded up to this count.
 constexpr int twiddle_entries(int n_freq) { return 128 + 2 * (n_freq / 64); }
-/// The four tables for n_freq, concatenated in that order (host, double
-/// precision rounded once to float).
+/// The tables for n_freq, concatenated in that order (host, double precision
+/// rounded once to float), twiddle_entries(n_freq) of them.
 void fengine_twiddles_host(int n_freq, std::vector<float2> *all);
 /// Point `tw` at the four tables stored concatenated from `base` (device memory).
 void twiddle_views(float2 *base, int n_freq, TwiddleTables *tw);

@@ -14,7 +14,9 @@
 //     z[n] = x[2n] + i*x[2n+1] and transformed by a Stockham autosort FFT in
 //     shared memory (three or four passes of radix 8..32, led by a radix-3, 5
 //     or 7 pass when M is not a power of two; FePlan below), FP32 in
-//     registers, twiddles from host-computed double-precision tables;
+//     registers, twiddles from host-computed double-precision tables; above
+//     n_freq 16384 the M points are first split into two M/2-point sequences
+//     (even and odd bins) that the CTA transforms in turn (HALF below);
 //   * the split X[k] = Fe[k] + w^k Fo[k] turns Z into the L-point real spectrum;
 //     bins 0..M-1 are written, the Nyquist bin M is dropped and nothing is
 //     normalised (reference semantics, HANDOFF.md:583-602).
@@ -40,7 +42,7 @@ namespace {
 // ---------------------------------------------------------------------------
 // Small DFTs in registers, forward sign (exp(-2*pi*i*n*k/R)), natural order.
 // The power-of-two radices' constant twiddles are 32nd roots of unity; the odd
-// radices 3, 5 and 7 (first pass of lengths 3, 5 or 7 x 2^k) use their own.
+// radices 3 .. 15 (first pass of lengths R x 2^k) use their own.
 // ---------------------------------------------------------------------------
 
 template <int R>
@@ -67,21 +69,49 @@ struct Dft<4> {
     }
 };
 
-// cos(2*pi*m/R) and sin(2*pi*m/R) for the odd radices R = 3, 5, 7 and
-// m = 1..(R-1)/2 (the values of the circle functions at those angles, to 21 digits).
+// cos(2*pi*m/R) and sin(2*pi*m/R) for the odd radices R = 3, 5, ..., 15 and
+// m = 1..(R-1)/2 (the values of the circle functions at those angles, to 21
+// digits). Radices 3, 5 and 7 lead the plans of lengths 3, 5, 7 x 2^k; 9, 11,
+// 13 and 15 those of the half-length sequences of n_freq 18432 .. 30720.
+__host__ __device__ constexpr float pick7(int m, float a1, float a2 = 0.f, float a3 = 0.f,
+                                          float a4 = 0.f, float a5 = 0.f, float a6 = 0.f,
+                                          float a7 = 0.f) {
+    return m == 1 ? a1 : m == 2 ? a2 : m == 3 ? a3 : m == 4 ? a4 : m == 5 ? a5 : m == 6 ? a6 : a7;
+}
 __host__ __device__ constexpr float cos_odd(int R, int m) {
     return R == 3 ? -0.5f
-         : R == 5 ? (m == 1 ? 0.309016994374947424102f : -0.809016994374947424102f)
-                  : (m == 1 ? 0.623489801858733530525f
-                   : m == 2 ? -0.222520933956314404289f
-                            : -0.900968867902419126236f);
+         : R == 5 ? pick7(m, 0.309016994374947424102f, -0.809016994374947424102f)
+         : R == 7 ? pick7(m, 0.623489801858733530525f, -0.222520933956314404289f,
+                          -0.900968867902419126236f)
+         : R == 9 ? pick7(m, 0.766044443118978035202f, 0.173648177666930348852f, -0.5f,
+                          -0.939692620785908384054f)
+         : R == 11 ? pick7(m, 0.841253532831181168862f, 0.415415013001886425529f,
+                           -0.142314838273285140444f, -0.654860733945285064057f,
+                           -0.95949297361449738989f)
+         : R == 13 ? pick7(m, 0.8854560256532098959f, 0.568064746731155802512f,
+                           0.120536680255323053349f, -0.35460488704253562597f,
+                           -0.748510748171101098635f, -0.970941817426052027157f)
+                   : pick7(m, 0.913545457642600895502f, 0.669130606358858213826f,
+                           0.309016994374947424102f, -0.1045284632676534714f, -0.5f,
+                           -0.809016994374947424102f, -0.978147600733805637929f);
 }
 __host__ __device__ constexpr float sin_odd(int R, int m) {
     return R == 3 ? 0.866025403784438646764f
-         : R == 5 ? (m == 1 ? 0.951056516295153572116f : 0.587785252292473129169f)
-                  : (m == 1 ? 0.781831482468029808708f
-                   : m == 2 ? 0.974927912181823607018f
-                            : 0.433883739117558120476f);
+         : R == 5 ? pick7(m, 0.951056516295153572116f, 0.587785252292473129169f)
+         : R == 7 ? pick7(m, 0.781831482468029808708f, 0.974927912181823607018f,
+                          0.433883739117558120476f)
+         : R == 9 ? pick7(m, 0.642787609686539326323f, 0.984807753012208059367f,
+                          0.866025403784438646764f, 0.342020143325668733044f)
+         : R == 11 ? pick7(m, 0.540640817455597582108f, 0.909631995354518371412f,
+                           0.989821441880932732376f, 0.755749574354258283774f,
+                           0.281732556841429697711f)
+         : R == 13 ? pick7(m, 0.464723172043768545656f, 0.82298386589365639458f,
+                           0.992708874098053992801f, 0.93501624268541482344f,
+                           0.663122658240795202377f, 0.239315664287557767149f)
+                   : pick7(m, 0.406736643075800207754f, 0.743144825477394235015f,
+                           0.951056516295153572116f, 0.994521895368273336923f,
+                           0.866025403784438646764f, 0.587785252292473129169f,
+                           0.207911690817759337102f);
 }
 
 // Odd R: the inputs n and R-n meet the same cosine and opposite sines, so with
@@ -106,9 +136,12 @@ struct DftOdd {
             float2 a = x0, b = make_float2(0.f, 0.f);
 #pragma unroll
             for (int n = 1; n <= H; ++n) {
-                const int m = (n * k) % R;   // angle 2*pi*m/R; beyond H the sine changes sign
-                const float c = cos_odd(R, m <= H ? m : R - m);
-                const float sn = m <= H ? sin_odd(R, m) : -sin_odd(R, R - m);
+                // angle 2*pi*m/R; beyond H the sine changes sign; for a composite
+                // R (9, 15) n*k can be a multiple of R: angle 0
+                const int m = (n * k) % R;
+                const int mm = m <= H ? m : R - m;
+                const float c = mm == 0 ? 1.0f : cos_odd(R, mm);
+                const float sn = mm == 0 ? 0.0f : m <= H ? sin_odd(R, mm) : -sin_odd(R, mm);
                 a = make_float2(fmaf(s[n - 1].x, c, a.x), fmaf(s[n - 1].y, c, a.y));
                 b = make_float2(fmaf(d[n - 1].x, sn, b.x), fmaf(d[n - 1].y, sn, b.y));
             }
@@ -121,6 +154,10 @@ struct DftOdd {
 template <> struct Dft<3> : DftOdd<3> {};
 template <> struct Dft<5> : DftOdd<5> {};
 template <> struct Dft<7> : DftOdd<7> {};
+template <> struct Dft<9> : DftOdd<9> {};
+template <> struct Dft<11> : DftOdd<11> {};
+template <> struct Dft<13> : DftOdd<13> {};
+template <> struct Dft<15> : DftOdd<15> {};
 
 // R = 4 x (R/4): n = (R/4)*n1 + n2, k = k1 + 4*k2.
 template <int R>
@@ -210,8 +247,17 @@ template <> struct FePlan<4096, 0> { static constexpr int R0 = 16, R1 = 16, R1b 
 template <> struct FePlan<2048, 0> { static constexpr int R0 = 16, R1 = 8, R1b = 1, R2 = 16; };
 template <> struct FePlan<1024, 0> { static constexpr int R0 = 16, R1 = 8, R1b = 1, R2 = 8; };
 template <> struct FePlan<512, 0> { static constexpr int R0 = 16, R1 = 4, R1b = 1, R2 = 8; };
+// Half lengths of n_freq 18432, 22528, 26624 and 30720 (the other half lengths
+// above, 10240 .. 16384, use their own plans).
+template <> struct FePlan<15360, 0> { static constexpr int R0 = 15, R1 = 16, R1b = 4, R2 = 16; };
+template <> struct FePlan<13312, 0> { static constexpr int R0 = 13, R1 = 16, R1b = 4, R2 = 16; };
+template <> struct FePlan<11264, 0> { static constexpr int R0 = 11, R1 = 16, R1b = 4, R2 = 16; };
+template <> struct FePlan<9216, 0> { static constexpr int R0 = 9, R1 = 16, R1b = 4, R2 = 16; };
 
-template <int MM, int PLAN>
+// HALF: MM is half of n_freq; a CTA holds the whole frame of 4*MM int8 samples
+// (one buffer: two would not fit beside the data) and transforms its two
+// half-length sequences one after the other.
+template <int MM, int PLAN, bool HALF = false>
 struct FeCfg {
     using Plan = FePlan<MM, PLAN>;
     static constexpr int M = MM;
@@ -224,10 +270,11 @@ struct FeCfg {
     static constexpr int PADSHIFT = (R0 == 32) ? 5 : 4;
     static constexpr int N_PASS_HI = M / 64;
     static constexpr int N_POST_HI = M / 64;
+    static constexpr int FRAME = HALF ? 4 * M : 2 * M;   // int8 bytes of one frame
     // shared memory layout (bytes)
-    static constexpr int OFF_X0 = 0;                   // int8 frame, buffer 0
-    static constexpr int OFF_X1 = 2 * M;               // int8 frame, buffer 1
-    static constexpr int OFF_D = 4 * M;                // padded complex data
+    static constexpr int OFF_X0 = 0;                      // int8 frame, buffer 0
+    static constexpr int OFF_X1 = HALF ? 0 : FRAME;       // int8 frame, buffer 1
+    static constexpr int OFF_D = HALF ? FRAME : 2 * FRAME;   // padded complex data
     static constexpr int OFF_PLO = OFF_D + (M + (M >> PADSHIFT)) * 8;
     static constexpr int OFF_PHI = OFF_PLO + 92 * 8;   // lo[64] + lo4[16] + lo8[8] + lo16[4]
     static constexpr int OFF_QLO = OFF_PHI + N_PASS_HI * 8;
@@ -235,7 +282,9 @@ struct FeCfg {
     static constexpr int OFF_T2 = OFF_QHI + N_POST_HI * 8;   // second-pass twiddles
     static constexpr int OFF_BAR = (OFF_T2 + R0 * R1 * 8 + 15) / 16 * 16;
     static constexpr int OFF_FLAG = OFF_BAR + 16;
+    static constexpr int OFF_SHIFT = OFF_FLAG + 8;        // HALF: odd_shift
     static constexpr int SMEM = OFF_FLAG + 16;
+    static_assert(SMEM <= 227 * 1024, "shared memory");
     // CTAs per SM the launch bounds plan for: as many as shared memory allows,
     // with at most 128 registers per thread (64 at 1024 threads).
     static constexpr int BY_SMEM = (220 * 1024) / SMEM;
@@ -272,21 +321,38 @@ __device__ __forceinline__ int mod_c(int j) {
     return static_cast<int>(static_cast<unsigned>(j) % static_cast<unsigned>(D));
 }
 
+// Where a pass reads its input: the data in shared memory, or (first pass)
+// the int8 frame: its M sample pairs as M complex points; or, for a frame of
+// 2M pairs split into two half-length sequences (one radix-2 step of
+// decimation in frequency, z = the 2M points), z[e] + z[e+M] (the sequence
+// whose transform is the even bins) or (z[e] - z[e+M]) * exp(-pi*i*e/M) (the
+// odd bins).
+enum PassSource : int { kFromShared = 0, kFromInt8 = 1, kFromInt8Sum = 2, kFromInt8Diff = 3 };
+
 // Stockham pass of radix R over M points with sub-transform size NS:
 //   out[(j/NS)*NS*R + j%NS + r*NS] = DFT_R( in[j + r*M/R] * w^(r*(j%NS)) )
 // for the M/R butterflies j. Each thread owns ceil(P/R) of them (j = tid + q*T);
 // where R does not divide P (an odd first radix) the last round of butterflies
 // is partial and the threads past M/R sit it out. In place: read all, barrier,
-// write all, barrier. The first pass reads int8 sample pairs instead of shared
-// data. TAB: the pass's twiddles w^(r*(j%NS)) (NS*R of them) come from table
-// `t2` laid out [r][j%NS] instead of from the two-level tables.
-template <int M, int T, int P, int R, int NS, int SHIFT, bool FIRST, bool TAB = false>
+// write all, barrier. The odd-radix first pass of a split frame (which also
+// combines two points and, for the odd bins, multiplies each by a twiddle)
+// reads the int8 frame, not the data it writes, so it instead waits once at
+// the start (for the previous transform's last reads of the data) and then
+// writes each butterfly as soon as it is computed, holding R values at a time
+// instead of ceil(P/R)*R. (The plain odd-radix first pass keeps the first
+// order: streaming it made n_freq 6144 5 % slower and 10240, 14336 no faster.)
+// TAB: the pass's twiddles w^(r*(j%NS)) (NS*R of them) come from table `t2`
+// laid out [r][j%NS] instead of from the two-level tables. qlo/qhi: the
+// exp(-pi*i*e/M) tables that kFromInt8Diff multiplies by.
+template <int M, int T, int P, int R, int NS, int SHIFT, int SRC, bool TAB = false>
 __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *__restrict__ sx,
                                          const float2 *lo, const float2 *hi, int tid,
-                                         const float2 *t2 = nullptr) {
+                                         const float2 *t2 = nullptr, const float2 *qlo = nullptr,
+                                         const float2 *qhi = nullptr) {
     constexpr int NB = (P + R - 1) / R;
     constexpr int STRIDE = M / R;
     constexpr bool EXACT = NB * R == P;   // NB*T == M/R: every thread has NB butterflies
+    constexpr bool STREAM = (SRC == kFromInt8Sum || SRC == kFromInt8Diff) && (R % 2 == 1);
     static_assert(M % (NS * R) == 0, "bad radix plan");
     // Reads: a padded per-thread base plus a compile-time offset, since the read
     // stride is a multiple of the padding period. Writes likewise when the write
@@ -297,43 +363,72 @@ __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *_
     constexpr bool RUNS = NS % (1 << SHIFT) == 0 || (NS == 1 && R == (1 << SHIFT));
     constexpr int PSTRIDE = STRIDE + (STRIDE >> SHIFT);
     constexpr int PNS = (NS == 1) ? 1 : NS + (NS >> SHIFT);
-    float2 v[NB][R];
+    const uint16_t *x16 = reinterpret_cast<const uint16_t *>(sx);
+    auto compute = [&](int j, float2 *v) {
+        if constexpr (SRC == kFromInt8) {
 #pragma unroll
-    for (int q = 0; q < NB; ++q) {
-        const int j = tid + q * T;
-        if (!EXACT && j >= STRIDE) continue;
-        if constexpr (FIRST) {
+            for (int r = 0; r < R; ++r) v[r] = int8_pair_to_float2(x16[j + r * STRIDE]);
+        } else if constexpr (SRC == kFromInt8Sum) {
 #pragma unroll
             for (int r = 0; r < R; ++r)
-                v[q][r] = int8_pair_to_float2(
-                    reinterpret_cast<const uint16_t *>(sx)[j + r * STRIDE]);
+                v[r] = cadd(int8_pair_to_float2(x16[j + r * STRIDE]),
+                            int8_pair_to_float2(x16[j + r * STRIDE + M]));
+        } else if constexpr (SRC == kFromInt8Diff) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int e = j + r * STRIDE;
+                v[r] = cmul(csub(int8_pair_to_float2(x16[e]), int8_pair_to_float2(x16[e + M])),
+                            cmul(qlo[e & 63], qhi[e >> 6]));
+            }
         } else {
             const int pj = padi<SHIFT>(j);
 #pragma unroll
-            for (int r = 0; r < R; ++r) v[q][r] = sd[pj + r * PSTRIDE];
+            for (int r = 0; r < R; ++r) v[r] = sd[pj + r * PSTRIDE];
         }
         if constexpr (TAB) {
             const float2 *tj = t2 + mod_c<NS>(j);
 #pragma unroll
-            for (int r = 1; r < R; ++r) v[q][r] = cmul(v[q][r], tj[r * NS]);
+            for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tj[r * NS]);
         } else if constexpr (NS > 1) {
-            apply_twiddles<R>(v[q], mod_c<NS>(j) * (M / (NS * R)), lo, hi);
+            apply_twiddles<R>(v, mod_c<NS>(j) * (M / (NS * R)), lo, hi);
         }
-        Dft<R>::run(v[q]);
-    }
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < NB; ++q) {
-        const int j = tid + q * T;
-        if (!EXACT && j >= STRIDE) continue;
+        Dft<R>::run(v);
+    };
+    auto store = [&](int j, const float2 *v) {
         const int base = div_c<NS>(j) * (NS * R) + mod_c<NS>(j);
         if constexpr (RUNS) {
             const int pb = padi<SHIFT>(base);
 #pragma unroll
-            for (int r = 0; r < R; ++r) sd[pb + r * PNS] = v[q][r];
+            for (int r = 0; r < R; ++r) sd[pb + r * PNS] = v[r];
         } else {
 #pragma unroll
-            for (int r = 0; r < R; ++r) sd[padi<SHIFT>(base + r * NS)] = v[q][r];
+            for (int r = 0; r < R; ++r) sd[padi<SHIFT>(base + r * NS)] = v[r];
+        }
+    };
+    if constexpr (STREAM) {
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+            const int j = tid + q * T;
+            if (!EXACT && j >= STRIDE) continue;
+            float2 v[R];
+            compute(j, v);
+            store(j, v);
+        }
+    } else {
+        float2 v[NB][R];
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+            const int j = tid + q * T;
+            if (!EXACT && j >= STRIDE) continue;
+            compute(j, v[q]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+            const int j = tid + q * T;
+            if (!EXACT && j >= STRIDE) continue;
+            store(j, v[q]);
         }
     }
     __syncthreads();
@@ -395,14 +490,54 @@ __device__ __forceinline__ void last_pass_store(const float2 *__restrict__ sd,
     if (t0) yrow.put(M / 2, make_float2(a[H].x * yrow.scale, -a[H].y * yrow.scale));
 }
 
+// Last pass for the odd bins of a frame split into two half-length sequences:
+// B[k'] = Z[2k'+1], k' < M (M = n_freq/2, this transform's length). Bin
+// k = 2k'+1 of the real spectrum pairs with n_freq - k = 2(M-1-k')+1, that is
+// B[k'] with B[M-1-k']; for k' = j + i*J the partner is butterfly J-1-j, output
+// R-1-i. Thread t owns butterflies t and J-1-t (t < J/2 = T), so its R pairs
+// are (a[i], b[R-1-i]) and no element pairs with itself. The split twiddle is
+// exp(-2*pi*i*k/(2*n_freq)) = exp(-pi*i*k'/M) * exp(-pi*i/n_freq) (odd_shift).
+// Row: a STEP 2 row of the odd bins, so index k' lands on bin 2k'+1.
+template <int MM, int PLAN, class Row>
+__device__ __forceinline__ void last_pass_store_odd(const float2 *__restrict__ sd,
+                                                    const float2 *plo, const float2 *phi,
+                                                    const float2 *qlo, const float2 *qhi,
+                                                    float2 odd_shift, const Row &yrow, int tid) {
+    using C = FeCfg<MM, PLAN>;
+    constexpr int M = C::M, J = C::J, R = C::R2;
+    static_assert(J % (1 << C::PADSHIFT) == 0 && J % 2 == 0, "last-pass stride");
+    constexpr int PJ = J + (J >> C::PADSHIFT);
+    const int j1 = tid, j2 = J - 1 - tid;
+    float2 a[R], b[R];
+    const int p1 = padi<C::PADSHIFT>(j1), p2 = padi<C::PADSHIFT>(j2);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        a[r] = sd[p1 + r * PJ];
+        b[r] = sd[p2 + r * PJ];
+    }
+    apply_twiddles<R>(a, j1, plo, phi);
+    apply_twiddles<R>(b, j2, plo, phi);
+    Dft<R>::run(a);   // a[r] = B[j1 + r*J]
+    Dft<R>::run(b);   // b[r] = B[j2 + r*J]
+    const float2 w1 = cmul(cmul(qlo[j1 & 63], qhi[j1 >> 6]), odd_shift);
+#pragma unroll
+    for (int i = 0; i < R; ++i)   // exp(-pi*i*i/R) = exp(-2*pi*i*i*(16/R)/32)
+        split_store(a[i], b[R - 1 - i], mul_w32(w1, i * (16 / R)), j1 + i * J, M - 1, true, yrow);
+}
+
 struct TwPtrs {
     const float2 *pass_lo, *pass_hi, *post_lo, *post_hi;
+    const float2 *odd_shift;   // HALF only
 };
 
-template <int MM, int PLAN, int FMT, bool CONTIG>
-__global__ void __launch_bounds__(FeCfg<MM, PLAN>::T, FeCfg<MM, PLAN>::MIN_BLOCKS)
+// HALF (n_freq = 2*MM above 16384): each item's frame of 2*MM sample pairs is
+// transformed as two MM-point sequences, even bins then odd bins, from one
+// int8 buffer; the next item's copy is issued once the second sequence's first
+// pass has read the frame, and lands during the rest of that transform.
+template <int MM, int PLAN, int FMT, bool CONTIG, bool HALF>
+__global__ void __launch_bounds__(FeCfg<MM, PLAN, HALF>::T, FeCfg<MM, PLAN, HALF>::MIN_BLOCKS)
     fengine_kernel(FengineArgs a, TwPtrs tw) {
-    using C = FeCfg<MM, PLAN>;
+    using C = FeCfg<MM, PLAN, HALF>;
     constexpr int M = C::M;
     constexpr int T = C::T;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -416,8 +551,10 @@ __global__ void __launch_bounds__(FeCfg<MM, PLAN>::T, FeCfg<MM, PLAN>::MIN_BLOCK
     float2 *t2 = reinterpret_cast<float2 *>(smem + C::OFF_T2);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + C::OFF_BAR);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + C::OFF_FLAG);
+    float2 *odd_shift = reinterpret_cast<float2 *>(smem + C::OFF_SHIFT);
 
     const int tid = threadIdx.x;
+    if (HALF && tid == 0) *odd_shift = *tw.odd_shift;
     for (int i = tid; i < 64; i += T) {
         plo[i] = tw.pass_lo[i];
         qlo[i] = tw.post_lo[i];
@@ -436,14 +573,14 @@ __global__ void __launch_bounds__(FeCfg<MM, PLAN>::T, FeCfg<MM, PLAN>::MIN_BLOCK
     }
     if (tid == 0) {
         mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        if (!HALF) mbar_init(&bar[1], 1);
         *abort_flag = 0;
         fence_mbar_init();
     }
     __syncthreads();
 
     const int n_items = a.frames * a.n_station;
-    const uint32_t frame_bytes = 2u * M;
+    const uint32_t frame_bytes = C::FRAME;
     const int ytile_shift = __ffs(a.ytile) - 1;
     const float out_scale = (FMT == kSpectraF32) ? 1.0f : a.y_scale;   // FP32 bins unscaled
     auto src_of = [&](int item) {
@@ -465,10 +602,10 @@ __global__ void __launch_bounds__(FeCfg<MM, PLAN>::T, FeCfg<MM, PLAN>::MIN_BLOCK
     uint32_t parity_bits = 0u;   // bit b = phase parity of bar[b]
 
     for (int n = 0; item < n_items; ++n, item += gridDim.x) {
-        const int buf = n & 1;
+        const int buf = HALF ? 0 : (n & 1);
         const int next = item + gridDim.x;
         bool next_issued = false;
-        if (tid == 0 && next < n_items && present(next)) {
+        if (!HALF && tid == 0 && next < n_items && present(next)) {
             // The other buffer was last read by the previous item's first pass,
             // which every thread finished before that pass's first barrier.
             fence_proxy_async_smem();
@@ -476,6 +613,15 @@ __global__ void __launch_bounds__(FeCfg<MM, PLAN>::T, FeCfg<MM, PLAN>::MIN_BLOCK
             bulk_copy_g2s(buf ? sx0 : sx1, src_of(next), frame_bytes, &bar[buf ^ 1]);
             next_issued = true;
         }
+        // HALF: the single buffer is free once this item's frame has been read
+        // (or at once, for a missing frame, which was never copied).
+        auto issue_next_into_buffer = [&] {
+            if (tid == 0 && next < n_items && present(next)) {
+                fence_proxy_async_smem();
+                mbar_arrive_expect_tx(&bar[0], frame_bytes);
+                bulk_copy_g2s(sx0, src_of(next), frame_bytes, &bar[0]);
+            }
+        };
         using Row = YRow<FMT, CONTIG>;
         const Row yrow{
             reinterpret_cast<typename Row::T *>(a.y) + static_cast<size_t>(item) * a.ytile,
@@ -483,8 +629,9 @@ __global__ void __launch_bounds__(FeCfg<MM, PLAN>::T, FeCfg<MM, PLAN>::MIN_BLOCK
             0.5f * out_scale};
 
         if (!present(item)) {
+            if constexpr (HALF) issue_next_into_buffer();
             // Missing frame: its samples count as zeros, so does its spectrum.
-            for (int k = tid; k < M; k += T) yrow.put(k, make_float2(0.f, 0.f));
+            for (int k = tid; k < (HALF ? 2 * M : M); k += T) yrow.put(k, make_float2(0.f, 0.f));
             continue;
         }
 
@@ -496,6 +643,32 @@ __global__ void __launch_bounds__(FeCfg<MM, PLAN>::T, FeCfg<MM, PLAN>::MIN_BLOCK
                                kErrFengineCopyTimeout))
             *abort_flag = 1;
         parity_bits ^= 1u << buf;
+
+        if constexpr (HALF) {
+            using RowH = YRow<FMT, CONTIG, 2>;
+            const RowH even{yrow.base, yrow.tile_stride, yrow.shift, yrow.scale, yrow.half, 0};
+            const RowH odd{yrow.base, yrow.tile_stride, yrow.shift, yrow.scale, yrow.half, 1};
+            fft_pass<M, T, C::P, C::R0, 1, C::PADSHIFT, kFromInt8Sum>(sd, sx0, plo, phi, tid,
+                                                                     nullptr, qlo, qhi);
+            if (*abort_flag) return;   // nothing in flight: the next copy is not issued yet
+            fft_pass<M, T, C::P, C::R1, C::R0, C::PADSHIFT, kFromShared, true>(sd, nullptr, plo,
+                                                                              phi, tid, t2);
+            if constexpr (C::R1b > 1)
+                fft_pass<M, T, C::P, C::R1b, C::R0 * C::R1, C::PADSHIFT, kFromShared>(
+                    sd, nullptr, plo, phi, tid);
+            last_pass_store<MM, PLAN>(sd, plo, phi, qlo, qhi, even, tid);
+            fft_pass<M, T, C::P, C::R0, 1, C::PADSHIFT, kFromInt8Diff>(sd, sx0, plo, phi, tid,
+                                                                      nullptr, qlo, qhi);
+            // that pass ended with a barrier: every thread has read the frame
+            issue_next_into_buffer();
+            fft_pass<M, T, C::P, C::R1, C::R0, C::PADSHIFT, kFromShared, true>(sd, nullptr, plo,
+                                                                              phi, tid, t2);
+            if constexpr (C::R1b > 1)
+                fft_pass<M, T, C::P, C::R1b, C::R0 * C::R1, C::PADSHIFT, kFromShared>(
+                    sd, nullptr, plo, phi, tid);
+            last_pass_store_odd<MM, PLAN>(sd, plo, phi, qlo, qhi, *odd_shift, odd, tid);
+            continue;
+        }
 
         if (a.pmask != nullptr) {
             // Lost packets count as zeros: clear them in the landed copy before
@@ -511,7 +684,7 @@ __global__ void __launch_bounds__(FeCfg<MM, PLAN>::T, FeCfg<MM, PLAN>::MIN_BLOCK
             }
         }
 
-        fft_pass<M, T, C::P, C::R0, 1, C::PADSHIFT, true>(sd, buf ? sx1 : sx0, plo, phi, tid);
+        fft_pass<M, T, C::P, C::R0, 1, C::PADSHIFT, kFromInt8>(sd, buf ? sx1 : sx0, plo, phi, tid);
         // the pass ends with a barrier: every thread sees the same flag
         if (*abort_flag) {
             // Let whatever copy is still in flight land before the CTA exits.
@@ -519,32 +692,32 @@ __global__ void __launch_bounds__(FeCfg<MM, PLAN>::T, FeCfg<MM, PLAN>::MIN_BLOCK
                 mbar_wait_bounded(&bar[buf ^ 1], (parity_bits >> (buf ^ 1)) & 1u, nullptr, 0);
             return;
         }
-        fft_pass<M, T, C::P, C::R1, C::R0, C::PADSHIFT, false, true>(sd, nullptr, plo, phi, tid,
-                                                                    t2);
+        fft_pass<M, T, C::P, C::R1, C::R0, C::PADSHIFT, kFromShared, true>(sd, nullptr, plo, phi,
+                                                                          tid, t2);
         if constexpr (C::R1b > 1)
-            fft_pass<M, T, C::P, C::R1b, C::R0 * C::R1, C::PADSHIFT, false>(sd, nullptr, plo, phi,
-                                                                          tid);
+            fft_pass<M, T, C::P, C::R1b, C::R0 * C::R1, C::PADSHIFT, kFromShared>(sd, nullptr, plo,
+                                                                                phi, tid);
         last_pass_store<MM, PLAN>(sd, plo, phi, qlo, qhi, yrow, tid);
         // The next item's first pass synchronises before it overwrites sd.
     }
 }
 
-template <int MM, int PLAN, int FMT, bool CONTIG>
+template <int MM, int PLAN, int FMT, bool CONTIG, bool HALF>
 corr_status launch_one(const FengineArgs &a, const TwiddleTables &tw, int num_sms,
                        cudaStream_t stream) {
-    using C = FeCfg<MM, PLAN>;
+    using C = FeCfg<MM, PLAN, HALF>;
     // Shared-memory limit and residency are per device: set up once on each.
     static PerDevice setup;
     static int per_sm[kMaxDeviceOrdinals];
     corr_status st = setup.run([](int dev) {
         corr_status s2 = cuda_check(
-            cudaFuncSetAttribute(fengine_kernel<MM, PLAN, FMT, CONTIG>,
+            cudaFuncSetAttribute(fengine_kernel<MM, PLAN, FMT, CONTIG, HALF>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM),
             "cudaFuncSetAttribute(fengine)");
         if (s2 != CORR_OK) return s2;
         int blocks = 0;
         s2 = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                            &blocks, fengine_kernel<MM, PLAN, FMT, CONTIG>, C::T, C::SMEM),
+                            &blocks, fengine_kernel<MM, PLAN, FMT, CONTIG, HALF>, C::T, C::SMEM),
                         "cudaOccupancyMaxActiveBlocksPerMultiprocessor(fengine)");
         if (s2 != CORR_OK) return s2;
         if (blocks < 1)
@@ -559,23 +732,24 @@ corr_status launch_one(const FengineArgs &a, const TwiddleTables &tw, int num_sm
     if (items <= 0) return CORR_OK;
     int grid = num_sms * per_sm[dev];
     if (grid > items) grid = items;
-    TwPtrs p{tw.pass_lo, tw.pass_hi, tw.post_lo, tw.post_hi};
-    fengine_kernel<MM, PLAN, FMT, CONTIG><<<grid, C::T, C::SMEM, stream>>>(a, p);
+    TwPtrs p{tw.pass_lo, tw.pass_hi, tw.post_lo, tw.post_hi, tw.odd_shift};
+    fengine_kernel<MM, PLAN, FMT, CONTIG, HALF><<<grid, C::T, C::SMEM, stream>>>(a, p);
     return cuda_check(cudaGetLastError(), "fengine_kernel launch");
 }
 
-template <int MM, int PLAN>
+template <int MM, int PLAN, bool HALF = false>
 corr_status launch_plan(const FengineArgs &a, const TwiddleTables &tw, int num_sms,
                         cudaStream_t stream) {
-    const bool contig = a.ytile == MM;
+    const bool contig = a.ytile == (HALF ? 2 * MM : MM);
     if (a.y_fmt == kSpectraF16)
-        return contig ? launch_one<MM, PLAN, kSpectraF16, true>(a, tw, num_sms, stream)
-                      : launch_one<MM, PLAN, kSpectraF16, false>(a, tw, num_sms, stream);
+        return contig ? launch_one<MM, PLAN, kSpectraF16, true, HALF>(a, tw, num_sms, stream)
+                      : launch_one<MM, PLAN, kSpectraF16, false, HALF>(a, tw, num_sms, stream);
     if (a.y_fmt == kSpectraF16Split)
-        return contig ? launch_one<MM, PLAN, kSpectraF16Split, true>(a, tw, num_sms, stream)
-                      : launch_one<MM, PLAN, kSpectraF16Split, false>(a, tw, num_sms, stream);
-    if (contig) return launch_one<MM, PLAN, kSpectraF32, true>(a, tw, num_sms, stream);
-    return launch_one<MM, PLAN, kSpectraF32, false>(a, tw, num_sms, stream);
+        return contig ? launch_one<MM, PLAN, kSpectraF16Split, true, HALF>(a, tw, num_sms, stream)
+                      : launch_one<MM, PLAN, kSpectraF16Split, false, HALF>(a, tw, num_sms,
+                                                                            stream);
+    if (contig) return launch_one<MM, PLAN, kSpectraF32, true, HALF>(a, tw, num_sms, stream);
+    return launch_one<MM, PLAN, kSpectraF32, false, HALF>(a, tw, num_sms, stream);
 }
 
 template <int MM>
@@ -590,6 +764,21 @@ corr_status launch_size(const FengineArgs &a, const TwiddleTables &tw, int num_s
     return launch_plan<MM, 0>(a, tw, num_sms, stream);
 }
 
+// n_freq = 2*MH above 16384: two MH-point transforms per frame.
+template <int MH>
+corr_status launch_half(const FengineArgs &a, const TwiddleTables &tw, int num_sms,
+                        cudaStream_t stream) {
+    if (a.fplan != 0)
+        return failf(CORR_ERR_ARG, "FFT plan %d is not available at n_freq=%d", a.fplan, 2 * MH);
+    if (a.pmask != nullptr)
+        return failf(CORR_ERR_ARG,
+                     "n_freq=%d: packet masks cover frames of at most 32 packets (n_freq <= 16384)",
+                     2 * MH);
+    if (tw.odd_shift == nullptr)
+        return failf(CORR_ERR_INTERNAL, "n_freq=%d: twiddle tables lack the odd-bin shift", 2 * MH);
+    return launch_plan<MH, 0, true>(a, tw, num_sms, stream);
+}
+
 } // namespace
 
 int fengine_plans(int n_freq) { return n_freq == 16384 ? 3 : 1; }
@@ -600,7 +789,7 @@ bool fengine_plan_ok(int n_freq, int fplan, int y_fmt) {
 }
 
 void fengine_twiddles_host(int n_freq, std::vector<float2> *all) {
-    const int M = n_freq;
+    const int M = fft_length(n_freq);
     const double pi = 3.14159265358979323846;
     auto cis = [](double a) {
         return make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
@@ -611,15 +800,19 @@ void fengine_twiddles_host(int n_freq, std::vector<float2> *all) {
     for (int u = 0; u < M / 64; ++u) all->push_back(cis(-2.0 * pi * 64.0 * u / M)); // pass_hi
     for (int u = 0; u < 64; ++u) all->push_back(cis(-pi * u / M));                  // post_lo
     for (int u = 0; u < M / 64; ++u) all->push_back(cis(-pi * 64.0 * u / M));       // post_hi
+    if (M != n_freq) all->push_back(cis(-pi / n_freq));                           // odd_shift
+    all->resize(static_cast<size_t>(twiddle_entries(n_freq)), make_float2(0.f, 0.f));
 }
 
 void twiddle_views(float2 *base, int n_freq, TwiddleTables *tw) {
-    tw->n_pass_hi = n_freq / 64;
-    tw->n_post_hi = n_freq / 64;
+    const int M = fft_length(n_freq);
+    tw->n_pass_hi = M / 64;
+    tw->n_post_hi = M / 64;
     tw->pass_lo = base;
     tw->pass_hi = base + 64;
     tw->post_lo = tw->pass_hi + tw->n_pass_hi;
     tw->post_hi = tw->post_lo + 64;
+    tw->odd_shift = M != n_freq ? tw->post_hi + tw->n_post_hi : nullptr;
 }
 
 corr_status fengine_prepare(int n_freq, TwiddleTables *tw) {
@@ -662,10 +855,18 @@ corr_status fengine_launch(int n_freq, const TwiddleTables &tw, const FengineArg
     case 12288: return launch_size<12288>(a, tw, num_sms, stream);
     case 14336: return launch_size<14336>(a, tw, num_sms, stream);
     case 16384: return launch_size<16384>(a, tw, num_sms, stream);
+    case 18432: return launch_half<9216>(a, tw, num_sms, stream);
+    case 20480: return launch_half<10240>(a, tw, num_sms, stream);
+    case 22528: return launch_half<11264>(a, tw, num_sms, stream);
+    case 24576: return launch_half<12288>(a, tw, num_sms, stream);
+    case 26624: return launch_half<13312>(a, tw, num_sms, stream);
+    case 28672: return launch_half<14336>(a, tw, num_sms, stream);
+    case 30720: return launch_half<15360>(a, tw, num_sms, stream);
+    case 32768: return launch_half<16384>(a, tw, num_sms, stream);
     default:
         return failf(CORR_ERR_ARG,
-                     "F-engine: n_freq=%d is neither a power of two in [512, 16384] nor a "
-                     "multiple of 2048 up to 16384",
+                     "F-engine: n_freq=%d is neither a power of two in [512, 32768] nor a "
+                     "multiple of 2048 up to 32768",
                      n_freq);
     }
 }

@@ -55,7 +55,9 @@ __device__ __forceinline__ float2 mul_w32(float2 a, int m) {
 // put() takes v already multiplied by `scale`: the real-FFT split folds it
 // into its factor 1/2 (half = scale/2), which is exact for the same reason.
 // CONTIG: ytile = n_freq, one contiguous row, bin k at base[k].
-template <int FMT, bool CONTIG>
+// STEP 2: the row takes every other bin, put(k) writing bin 2k + odd (the even
+// or the odd bins of a frame transformed as two half-length sequences).
+template <int FMT, bool CONTIG, int STEP = 1>
 struct YRow {
     using T = typename std::conditional<
         FMT == kSpectraF32, float2,
@@ -65,7 +67,9 @@ struct YRow {
     int shift;             // log2(ytile)
     float scale;
     float half;            // scale / 2
+    int odd = 0;           // STEP 2: 0 = even bins, 1 = odd bins
     __device__ __forceinline__ void put(int k, float2 v) const {
+        if constexpr (STEP == 2) k = 2 * k + odd;
         T *dst = CONTIG ? base + k
                         : base + (static_cast<uint32_t>(k >> shift) * tile_stride +
                                   static_cast<uint32_t>(k & ((1 << shift) - 1)));

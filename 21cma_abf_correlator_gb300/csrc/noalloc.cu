@@ -11,7 +11,7 @@
 // transform length live in a second fixed array.
 //
 // Properties a caller must know:
-//   * scratch: kNoAllocScratchBytes (64 MiB) of spectra plus 28 KB of twiddle
+//   * scratch: kNoAllocScratchBytes (64 MiB) of spectra plus 86 KB of twiddle
 //     tables, held by every GPU that loads the library until the process exits;
 //   * one call may cover at most 64 MiB / (n_station * n_freq * e) frames, e the
 //     bytes a spectrum bin takes between the engines (4 for the FP16 tensor
@@ -40,7 +40,8 @@ namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;
 // The transform lengths the F-engine takes, each with its tables in the array.
-constexpr int kSizes[] = {512, 1024, 2048, 4096, 6144, 8192, 10240, 12288, 14336, 16384};
+constexpr int kSizes[] = {512,   1024,  2048,  4096,  6144,  8192,  10240, 12288, 14336,
+                          16384, 18432, 20480, 22528, 24576, 26624, 28672, 30720, 32768};
 constexpr int kNumSizes = static_cast<int>(sizeof(kSizes) / sizeof(kSizes[0]));
 
 // Offset of the twiddle tables of kSizes[i] channels in the twiddle array.

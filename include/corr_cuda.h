@@ -81,10 +81,10 @@ typedef enum corr_status {
  *   abi_version == CORR_ABI_VERSION and struct_size == sizeof(corr_config)
  *                                              (else CORR_ERR_ABI)
  *   n_station >= 1 and n_station*(n_station+1)/2 <= 1024
- *   n_freq a multiple of 2048 up to 16384, as the reference requires (a
+ *   n_freq a multiple of 2048 up to 32768, as the reference requires (a
  *       frame must be whole 4096-sample packets), or 512 or 1024 (the engine
  *       only needs a transform length it has a plan for). Multiples of 2048
- *       above 16384 return CORR_ERR_NOT_IMPL, everything else CORR_ERR_ARG.
+ *       above 32768 return CORR_ERR_NOT_IMPL, everything else CORR_ERR_ARG.
  *   frames_per_slot >= 1, 1 <= chunk_frames <= frames_per_slot
  *   block_slots >= 2, rows_per_fetch >= 1
  *   the device ordinal(s) exist and are distinct; the split gives every

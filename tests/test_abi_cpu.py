@@ -153,10 +153,10 @@ def _cfg(pkg, **kw):
     (dict(abi_version=8), 2),              # CORR_ERR_ABI
     (dict(struct_size=72), 2),
     (dict(n_freq=4096 + 1024), 1),         # not a power of two / multiple of 2048
-    (dict(n_freq=18432), 8),               # multiple of 2048 above 16384: NOT_IMPL
+    (dict(n_freq=34816), 8),               # multiple of 2048 above 32768: NOT_IMPL
     (dict(n_freq=3072), 1),                # neither a power of two nor a multiple of 2048
     (dict(n_freq=256), 1),
-    (dict(n_freq=32768), 8),
+    (dict(n_freq=65536), 8),
     (dict(block_slots=1), 1),
     (dict(chunk_frames=17), 1),            # > frames_per_slot
     (dict(chunk_frames=0), 1),

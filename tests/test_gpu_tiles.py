@@ -85,12 +85,14 @@ def test_plain_layouts_are_bit_identical(pkg, cuda, oracle, ytile):
     assert oracle.rel_rms(got, oracle.correlate(x, present)) < 1e-5
 
 
+@pytest.mark.parametrize("nf", [10240, 20480])
 @pytest.mark.parametrize("xmode,ytile", [(0, 32), (0, 2048), (1, 8), (2, 4)])
-def test_layouts_at_a_length_that_is_not_a_power_of_two(pkg, cuda, oracle, xmode, ytile):
-    """n_freq 10240 = 5 x 2048: channel tiles of a power of two that divides it
-    give the same bits as contiguous rows (plain form: any such width; tensor
-    forms: their own tile width)."""
-    n, nf, frames = 6, 10240, 24
+def test_layouts_at_a_length_that_is_not_a_power_of_two(pkg, cuda, oracle, xmode, ytile, nf):
+    """n_freq 10240 = 5 x 2048, and 20480, whose frames are transformed as two
+    half-length sequences writing every other bin: channel tiles of a power of
+    two that divides n_freq give the same bits as contiguous rows (plain form:
+    any such width; tensor forms: their own tile width)."""
+    n, frames = 6, 24
     x, present, mask = _case(n, nf, frames, 10)
     base = _run(pkg, cuda, x, mask, xmode, None)
     if xmode:

@@ -84,10 +84,12 @@ def test_chunk_and_slot_boundaries_do_not_matter(pkg, cuda, oracle, synth):
 
 @pytest.mark.parametrize("xmode", [0, 1, 2])
 @pytest.mark.parametrize("n_freq", [512, 1024, 2048, 4096, 6144, 8192, 10240, 12288, 14336,
-                                    16384])
+                                    16384, 18432, 20480, 22528, 24576, 26624, 28672, 30720,
+                                    32768])
 def test_every_transform_length(pkg, cuda, oracle, n_freq, xmode):
     """Every F-engine size, writing each spectra format (FP32, FP16, FP16 hi/lo):
-    the powers of two and the multiples of 2048 that are 3, 5 or 7 x 2^k."""
+    the powers of two, the multiples of 2048 that are 3, 5 or 7 x 2^k, and those
+    above 16384, whose frames are transformed as two half-length sequences."""
     torch = cuda
     rng = np.random.default_rng(n_freq)
     n, frames = 3, 5
@@ -105,7 +107,7 @@ def test_every_transform_length(pkg, cuda, oracle, n_freq, xmode):
     eng.close()
 
 
-@pytest.mark.parametrize("n_freq", [6144, 10240, 12288, 14336])
+@pytest.mark.parametrize("n_freq", [6144, 10240, 12288, 14336, 18432, 26624, 32768])
 def test_abi_at_multiples_of_2048(pkg, cuda, oracle, n_freq):
     """The reference takes any multiple of 2048 (corr-cuda/src/corr_cuda.cpp:501-509):
     rows through the C ABI at the lengths that are not powers of two, with

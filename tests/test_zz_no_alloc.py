@@ -101,11 +101,11 @@ def test_fp16_form_holds_twice_the_frames(pkg, cuda):
 
 def test_calls_of_different_lengths_in_a_row(pkg, cuda):
     """Each transform length reads its own twiddle tables: 4096, 16384, 512,
-    6144 and 14336 channels back to back on one stream, each equal to the
-    allocating path."""
+    6144, 14336, 32768 and 22528 channels back to back on one stream, each equal
+    to the allocating path."""
     torch = cuda
     rng = np.random.default_rng(11)
-    for nf in (4096, 16384, 512, 6144, 14336, 4096):
+    for nf in (4096, 16384, 512, 6144, 14336, 32768, 22528, 4096):
         n, frames = 6, 16
         x = torch.from_numpy(rng.integers(-60, 61, size=(n, frames, 2 * nf)).astype(np.int8)).cuda()
         got = torch.zeros((n * (n + 1) // 2, nf), dtype=torch.complex64, device="cuda")
