@@ -94,8 +94,8 @@ struct TwiddleTables {
 };
 
 /// Spectra layout shared by the F- and X-engines: channel tiles of `ytile`
-/// channels (a power of two in [2, n_freq]), each tile holding every frame and
-/// station,
+/// channels (n_freq itself, or a power of two >= 2 that divides n_freq), each
+/// tile holding every frame and station,
 ///   y[((c / ytile) * y_frames + f) * n_station + s) * ytile + c % ytile]
 /// ytile = n_freq is one contiguous row of n_freq bins per (frame, station)
 /// (the F-engine's cheapest store pattern); ytile equal to the tensor
@@ -118,8 +118,9 @@ inline int spectra_format(int xmode) {
 }
 
 /// The power of two that FP16 spectra are scaled by: spectra of int8 frames
-/// satisfy |Y| <= 128*L, so 2^-(log2 L - 8) keeps every bin below 2^15, inside
-/// FP16's range, for every input; products are unscaled by its inverse square.
+/// satisfy |Y| <= 128*L, so 2^-(ceil(log2 L) - 8) keeps every bin at or below
+/// 2^15, inside FP16's range, for every input; products are unscaled by its
+/// inverse square.
 inline float spectra_scale(int n_freq) {
     int l = 0;
     while ((1 << l) < 2 * n_freq) ++l;

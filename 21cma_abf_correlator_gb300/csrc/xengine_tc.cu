@@ -15,8 +15,9 @@
 //   FP16 split : D = Dh + Dl, Dh = fp16(D), Dl = fp16(D - Dh) (about 22 bits);
 //                S ~ H + P + P^T with H = Dh^T Dh and P = Dl^T Dh (Dl^T Dl dropped).
 // Scale: spectra of int8 frames satisfy |Y| <= 128*L, so multiplying by the
-// power of two 2^-(log2 L - 8) keeps every value below 2^15 (< FP16 max) in
-// every channel for every input; being a power of two it is undone exactly.
+// power of two 2^-(ceil(log2 L) - 8) keeps every value at or below 2^15
+// (< FP16 max) in every channel for every input; being a power of two it is
+// undone exactly.
 // The int8 quantisation floor keeps |Y| >= ~sqrt(L/12) in every channel of real
 // data, so the scaled values sit in FP16's normal range and no per-channel
 // adaptive scale is needed.
