@@ -65,6 +65,10 @@ WORKLOADS = {
     "stream-40in-nf16384": Workload("stream-40in-nf16384", 40, 16384, 4096, 24.0, 0.2, 127,
                                     tones=((3000, 8.0, 10), (9000, 8.0, 10)), loss=0.002,
                                     seed=1005),
+    # Beyond the specification's five: the longest frames accepted (n_freq 32768,
+    # 65536-sample frames, transformed as two half-length sequences).
+    "wide-24in-nf32768": Workload("wide-24in-nf32768", 24, 32768, 2048, 24.0, 0.2, 63,
+                                  seed=1006),
 }
 
 
