@@ -5,7 +5,8 @@
 //     acc[b][c] += sum_f Y_j[f][c] * conj(Y_k[f][c])
 // with the reference's complex multiply-accumulate convention
 //     re += xr*yr + xi*yi,  im += xi*yr - xr*yi          (kernels.cu:243-245)
-// in FP32.
+// in FP32, as two fused multiply-adds per component (one rounding each),
+// issued as packed FP32x2 instructions.
 //
 // Shape: a CTA owns a tile of 32 channels (lane = channel) and a group of 4x4
 // station blocks (warp = block pair). Spectra for a few frames of every
@@ -105,13 +106,21 @@ __global__ void __launch_bounds__(1024, 1)
                     xj[i] = fr[(bj * kBlk + i) * kXch];
                     xk[i] = fr[(bk * kBlk + i) * kXch];
                 }
+                // a += xj * conj(xk) as two packed FMAs per pair:
+                //   (re, im) += (xj.x, xj.y) * (xk.x, xk.x)
+                //   (re, im) += (xj.y, -xj.x) * (xk.y, xk.y)
+                // the swapped and broadcast operands built once per station
+                float2 xjs[kBlk];
 #pragma unroll
-                for (int i = 0; i < kBlk; ++i)
+                for (int i = 0; i < kBlk; ++i) xjs[i] = make_float2(xj[i].y, -xj[i].x);
 #pragma unroll
-                    for (int l = 0; l < kBlk; ++l) {
-                        a[i][l].x += xj[i].x * xk[l].x + xj[i].y * xk[l].y;
-                        a[i][l].y += xj[i].y * xk[l].x - xj[i].x * xk[l].y;
-                    }
+                for (int l = 0; l < kBlk; ++l) {
+                    const float2 kx = make_float2(xk[l].x, xk[l].x);
+                    const float2 ky = make_float2(xk[l].y, xk[l].y);
+#pragma unroll
+                    for (int i = 0; i < kBlk; ++i)
+                        a[i][l] = fma2(xjs[i], ky, fma2(xj[i], kx, a[i][l]));
+                }
             }
         }
     }
