@@ -17,6 +17,7 @@
 // shared-memory load four multiply-accumulates.
 
 #include <algorithm>
+#include <type_traits>
 
 #include "engine.h"
 #include "ptx.cuh"
@@ -97,31 +98,41 @@ __global__ void __launch_bounds__(1024, 1)
         cp_async_commit();
         if (active) {
             const float2 *st = xs + (s % kXstages) * stage_elems;
+            // A warp whose two blocks are the same keeps only j <= k: it loads
+            // one block and skips the pairs below the diagonal (uniform per warp).
+            auto stage = [&](auto diag) {
+                constexpr bool DIAG = decltype(diag)::value;
 #pragma unroll
-            for (int fi = 0; fi < kXfs; ++fi) {
-                const float2 *fr = st + fi * npad * kXch + lane;
-                float2 xj[kBlk], xk[kBlk];
+                for (int fi = 0; fi < kXfs; ++fi) {
+                    const float2 *fr = st + fi * npad * kXch + lane;
+                    float2 xj[kBlk], xk[kBlk];
 #pragma unroll
-                for (int i = 0; i < kBlk; ++i) {
-                    xj[i] = fr[(bj * kBlk + i) * kXch];
-                    xk[i] = fr[(bk * kBlk + i) * kXch];
+                    for (int i = 0; i < kBlk; ++i) {
+                        xj[i] = fr[(bj * kBlk + i) * kXch];
+                        xk[i] = DIAG ? xj[i] : fr[(bk * kBlk + i) * kXch];
+                    }
+                    // a += xj * conj(xk) as two packed FMAs per pair:
+                    //   (re, im) += (xj.x, xj.y) * (xk.x, xk.x)
+                    //   (re, im) += (xj.y, -xj.x) * (xk.y, xk.y)
+                    // the swapped and broadcast operands built once per station
+                    float2 xjs[kBlk];
+#pragma unroll
+                    for (int i = 0; i < kBlk; ++i) xjs[i] = make_float2(xj[i].y, -xj[i].x);
+#pragma unroll
+                    for (int l = 0; l < kBlk; ++l) {
+                        const float2 kx = make_float2(xk[l].x, xk[l].x);
+                        const float2 ky = make_float2(xk[l].y, xk[l].y);
+#pragma unroll
+                        for (int i = 0; i < kBlk; ++i)
+                            if (!DIAG || i <= l)
+                                a[i][l] = fma2(xjs[i], ky, fma2(xj[i], kx, a[i][l]));
+                    }
                 }
-                // a += xj * conj(xk) as two packed FMAs per pair:
-                //   (re, im) += (xj.x, xj.y) * (xk.x, xk.x)
-                //   (re, im) += (xj.y, -xj.x) * (xk.y, xk.y)
-                // the swapped and broadcast operands built once per station
-                float2 xjs[kBlk];
-#pragma unroll
-                for (int i = 0; i < kBlk; ++i) xjs[i] = make_float2(xj[i].y, -xj[i].x);
-#pragma unroll
-                for (int l = 0; l < kBlk; ++l) {
-                    const float2 kx = make_float2(xk[l].x, xk[l].x);
-                    const float2 ky = make_float2(xk[l].y, xk[l].y);
-#pragma unroll
-                    for (int i = 0; i < kBlk; ++i)
-                        a[i][l] = fma2(xjs[i], ky, fma2(xj[i], kx, a[i][l]));
-                }
-            }
+            };
+            if (bj == bk)
+                stage(std::true_type{});
+            else
+                stage(std::false_type{});
         }
     }
     cp_async_wait<0>();
