@@ -9,7 +9,7 @@
 // issued as packed FP32x2 instructions.
 //
 // Shape: a CTA owns a tile of 32 channels (lane = channel) and a group of 4x4
-// station blocks (warp = block pair). Spectra for a few frames of every
+// station blocks (warp = block pair). Spectra for 4 to 12 frames of every
 // station in the tile are staged in shared memory by a 3-deep cp.async ring;
 // each thread keeps 16 complex accumulators in registers for the whole launch
 // and adds them into the row once at the end. Unlike the reference (one thread
@@ -26,8 +26,11 @@ namespace corrgb {
 namespace {
 
 constexpr int kXch = 32;     // channels per CTA, one per lane
-constexpr int kXfs = 4;      // frames per pipeline stage
 constexpr int kXstages = 3;  // cp.async ring depth
+// frames per pipeline stage: as many of 12, 8, 4 as three stages fit in shared
+// memory (12 up to 24 padded stations, 8 up to 36); fewer stages mean fewer
+// CTA barriers
+constexpr int kXfsWidest = 12, kXfsWide = 8, kXfsNarrow = 4;
 constexpr int kBlk = 4;      // stations per block
 
 __device__ __forceinline__ void decode_pair(int p, int nb, int *bj, int *bk) {
@@ -40,6 +43,7 @@ __device__ __forceinline__ void decode_pair(int p, int nb, int *bj, int *bk) {
     *bk = j + p;
 }
 
+template <int kXfs>
 __global__ void __launch_bounds__(1024, 1)
     xengine_plain_kernel(const float2 *__restrict__ y, int y_frames, int ytile, int n_station,
                          int npad, int n_freq, int frames, void *__restrict__ acc,
@@ -271,19 +275,31 @@ corr_status xengine_plain_launch(const XengineArgs &a, int num_sms, cudaStream_t
     const int n_pairs = nb * (nb + 1) / 2;
     const int groups = (n_pairs + 31) / 32;
     const int per_cta = (n_pairs + groups - 1) / groups;
-    const size_t smem = static_cast<size_t>(kXstages) * kXfs * npad * kXch * sizeof(float2);
+    const size_t per_frame = static_cast<size_t>(kXstages) * npad * kXch * sizeof(float2);
+    const int fs = per_frame * kXfsWidest <= 227 * 1024 ? kXfsWidest
+                 : per_frame * kXfsWide <= 227 * 1024   ? kXfsWide
+                                                        : kXfsNarrow;
+    const size_t smem = per_frame * fs;
     static PerDevice setup;   // the shared-memory limit is a per-device setting
     corr_status st = setup.run([](int) {
-        return cuda_check(cudaFuncSetAttribute(xengine_plain_kernel,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               227 * 1024),
-                          "cudaFuncSetAttribute(xengine_plain)");
+        for (auto k : {xengine_plain_kernel<kXfsWidest>, xengine_plain_kernel<kXfsWide>,
+                       xengine_plain_kernel<kXfsNarrow>}) {
+            corr_status s2 =
+                cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                227 * 1024),
+                           "cudaFuncSetAttribute(xengine_plain)");
+            if (s2 != CORR_OK) return s2;
+        }
+        return CORR_OK;
     });
     if (st != CORR_OK) return st;
     dim3 grid(groups, a.n_freq / kXch);
-    xengine_plain_kernel<<<grid, per_cta * 32, smem, stream>>>(
-        a.y, a.y_frames, a.ytile, a.n_station, npad, a.n_freq, a.frames, a.acc, a.acc64, per_cta,
-        n_pairs);
+    auto k = fs == kXfsWidest ? xengine_plain_kernel<kXfsWidest>
+           : fs == kXfsWide   ? xengine_plain_kernel<kXfsWide>
+                              : xengine_plain_kernel<kXfsNarrow>;
+    k<<<grid, per_cta * 32, smem, stream>>>(a.y, a.y_frames, a.ytile, a.n_station, npad,
+                                            a.n_freq, a.frames, a.acc, a.acc64, per_cta,
+                                            n_pairs);
     return cuda_check(cudaGetLastError(), "xengine_plain_kernel launch");
 }
 
