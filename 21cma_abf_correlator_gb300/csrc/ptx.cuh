@@ -141,6 +141,19 @@ __device__ __forceinline__ float2 cadd(float2 a, float2 b) {
     return d;
 }
 
+// d = a * b lane by lane as one packed FP32x2 multiply (sm_100+).
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 pa, pb, pd;\n\t"
+        "mov.b64 pa, {%2, %3};\n\t"
+        "mov.b64 pb, {%4, %5};\n\t"
+        "mul.rn.f32x2 pd, pa, pb;\n\t"
+        "mov.b64 {%0, %1}, pd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+
 // d = a * b + c lane by lane as one packed FP32x2 fused multiply-add (sm_100+):
 // each lane is the IEEE fma of the scalar instruction, in half the issue slots.
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {

@@ -5,8 +5,8 @@
 //     acc[b][c] += sum_f Y_j[f][c] * conj(Y_k[f][c])
 // with the reference's complex multiply-accumulate convention
 //     re += xr*yr + xi*yi,  im += xi*yr - xr*yi          (kernels.cu:243-245)
-// in FP32, as two fused multiply-adds per component (one rounding each),
-// issued as packed FP32x2 instructions.
+// in FP32 and in that order (the product pair rounded, then added to the
+// accumulator), issued as packed FP32x2 instructions.
 //
 // Shape: a CTA owns a tile of 32 channels (lane = channel) and a group of 4x4
 // station blocks (warp = block pair). Spectra for 4 to 12 frames of every
@@ -115,9 +115,11 @@ __global__ void __launch_bounds__(1024, 1)
                         xj[i] = fr[(bj * kBlk + i) * kXch];
                         xk[i] = DIAG ? xj[i] : fr[(bk * kBlk + i) * kXch];
                     }
-                    // a += xj * conj(xk) as two packed FMAs per pair:
-                    //   (re, im) += (xj.x, xj.y) * (xk.x, xk.x)
-                    //   (re, im) += (xj.y, -xj.x) * (xk.y, xk.y)
+                    // a += xj * conj(xk) in the reference's rounding order (the
+                    // pair's product, then one add to the accumulator), packed:
+                    //   t = (xj.x, xj.y) * (xk.x, xk.x)
+                    //   t = (xj.y, -xj.x) * (xk.y, xk.y) + t
+                    //   (re, im) += t
                     // the swapped and broadcast operands built once per station
                     float2 xjs[kBlk];
 #pragma unroll
@@ -129,7 +131,7 @@ __global__ void __launch_bounds__(1024, 1)
 #pragma unroll
                         for (int i = 0; i < kBlk; ++i)
                             if (!DIAG || i <= l)
-                                a[i][l] = fma2(xjs[i], ky, fma2(xj[i], kx, a[i][l]));
+                                a[i][l] = cadd(a[i][l], fma2(xjs[i], ky, mul2(xj[i], kx)));
                     }
                 }
             };
