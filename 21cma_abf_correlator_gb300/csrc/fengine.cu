@@ -12,11 +12,11 @@
 //     as zeros, which is what zeroing the samples and transforming them gives;
 //   * the real frame x[0..L) (L = 2M) is packed as M complex points
 //     z[n] = x[2n] + i*x[2n+1] and transformed by a Stockham autosort FFT in
-//     shared memory (three or four passes of radix 8..32, led by a radix-3, 5
-//     or 7 pass when M is not a power of two; FePlan below), FP32 in
+//     shared memory (three or four passes of radix 4..32, led by an odd radix
+//     3..15 when M is not a power of two; FePlan in fengine_impl.cuh), FP32 in
 //     registers, twiddles from host-computed double-precision tables; above
 //     n_freq 16384 the M points are first split into two M/2-point sequences
-//     (even and odd bins) that the CTA transforms in turn (HALF below);
+//     (even and odd bins) that the CTA transforms in turn (HALF);
 //   * the split X[k] = Fe[k] + w^k Fo[k] turns Z into the L-point real spectrum;
 //     bins 0..M-1 are written, the Nyquist bin M is dropped and nothing is
 //     normalised (reference semantics, HANDOFF.md:583-602).
