@@ -223,7 +223,17 @@ corr_status validate(const corr_config *cfg) {
         return failf(CORR_ERR_ARG, "block_slots=%d must be >= 2", cfg->block_slots);
     if (cfg->rows_per_fetch < 1)
         return failf(CORR_ERR_ARG, "rows_per_fetch=%d must be >= 1", cfg->rows_per_fetch);
-    return CORR_OK;
+    // The reference's per-device baseline limit, on the placement the split
+    // gives the configured devices (host-only: the ordinals are labels here).
+    std::vector<int> ordinals;
+    if (cfg->n_devices > 0)
+        ordinals.assign(cfg->devices, cfg->devices + cfg->n_devices);
+    else
+        ordinals.push_back(cfg->device_id);
+    std::vector<DevicePlacement> plan;
+    if ((st = plan_devices(cfg->n_station, cfg->split_mode, ordinals, &plan)) != CORR_OK)
+        return st;
+    return check_device_baselines(plan);
 }
 
 // The configured device list, checked against what is visible and mapped to

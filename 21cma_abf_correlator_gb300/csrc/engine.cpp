@@ -59,11 +59,9 @@ static bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
 
 corr_status check_geometry(int n_station, int n_freq) {
     if (n_station < 1) return fail(CORR_ERR_ARG, "n_station must be >= 1");
-    if (n_station * (n_station + 1) / 2 > 1024)
-        return failf(CORR_ERR_ARG,
-                     "n_station=%d gives %d baselines; at most 1024 (n_station <= 44) "
-                     "are supported",
-                     n_station, n_station * (n_station + 1) / 2);
+    if (n_station > kMaxStations)
+        return failf(CORR_ERR_ARG, "n_station=%d: an engine correlates at most %d stations",
+                     n_station, kMaxStations);
     if (n_freq < 1) return fail(CORR_ERR_ARG, "n_freq must be >= 1");
     // Powers of two from 512, and the reference's multiples of 2048 (frames of
     // whole 4096-sample packets), up to 32768: the F-engine's transform lengths.

@@ -264,6 +264,15 @@ corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_s
 corr_status fxplan_check(FxPlan *p);
 
 /// Host-side validation shared by corr_create and corrx_create.
+/// Stations one engine can correlate: the plain X-engine stages every station's
+/// spectra for a tile of channels in shared memory (two frames a stage at 128);
+/// the tensor forms take up to 64 (xengine_tc_default_shape).
+constexpr int kMaxStations = 128;
+/// Baselines the ABI lets one device own, the reference's per-device limit
+/// (corr-cuda/src/kernels.cu:474-483): 44 stations on one device; more only
+/// with the baselines split over several devices.
+constexpr int kMaxBaselinesPerDevice = 1024;
+/// n_station in [1, kMaxStations] and an n_freq the F-engine transforms.
 corr_status check_geometry(int n_station, int n_freq);
 
 } // namespace corrgb

@@ -174,6 +174,17 @@ corr_status plan_devices(int n_station, int split_mode, const std::vector<int> &
     return CORR_OK;
 }
 
+corr_status check_device_baselines(const std::vector<DevicePlacement> &plan) {
+    for (size_t d = 0; d < plan.size(); ++d)
+        if (plan[d].baselines.size() > static_cast<size_t>(kMaxBaselinesPerDevice))
+            return failf(CORR_ERR_ARG,
+                         "device index %zu would own %zu baselines; at most %d per device "
+                         "(n_station <= 44 on one device; split the baselines over more "
+                         "devices)",
+                         d, plan[d].baselines.size(), kMaxBaselinesPerDevice);
+    return CORR_OK;
+}
+
 bool placement_is_identity(const DevicePlacement &pl, int n_station) {
     const size_t nb = static_cast<size_t>(n_station) * (n_station + 1) / 2;
     if (pl.stations.size() != static_cast<size_t>(n_station) || pl.baselines.size() != nb)
@@ -207,8 +218,8 @@ extern "C" corr_status corrx_plan_query(const corr_config *cfg, int32_t device_i
     if (cfg->n_devices < 0 || cfg->n_devices > static_cast<int32_t>(CORR_MAX_DEVICES))
         return failf(CORR_ERR_ARG, "n_devices=%d outside [0, %u]", cfg->n_devices,
                      CORR_MAX_DEVICES);
-    if (cfg->n_station < 1 || cfg->n_station * (cfg->n_station + 1) / 2 > 1024)
-        return fail(CORR_ERR_ARG, "n_station must be in [1, 44]");
+    if (cfg->n_station < 1 || cfg->n_station > kMaxStations)
+        return failf(CORR_ERR_ARG, "n_station must be in [1, %d]", kMaxStations);
     std::vector<int> ordinals;
     if (cfg->n_devices > 0)
         ordinals.assign(cfg->devices, cfg->devices + cfg->n_devices);
@@ -217,6 +228,7 @@ extern "C" corr_status corrx_plan_query(const corr_config *cfg, int32_t device_i
     std::vector<DevicePlacement> plan;
     corr_status st = plan_devices(cfg->n_station, cfg->split_mode, ordinals, &plan);
     if (st != CORR_OK) return st;
+    if ((st = check_device_baselines(plan)) != CORR_OK) return st;
     if (device_index < 0 || device_index >= static_cast<int32_t>(plan.size()))
         return failf(CORR_ERR_ARG, "device_index %d out of range [0,%zu)", device_index,
                      plan.size());

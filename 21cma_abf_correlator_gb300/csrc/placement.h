@@ -36,6 +36,11 @@ struct DevicePlacement {
 corr_status plan_devices(int n_station, int split_mode, const std::vector<int> &ordinals,
                          std::vector<DevicePlacement> *out);
 
+/// The reference's per-device limit (corr-cuda/src/kernels.cu:474-483): every
+/// device owns at most kMaxBaselinesPerDevice baselines, so a run of more than
+/// 44 stations needs its baselines split over several devices.
+corr_status check_device_baselines(const std::vector<DevicePlacement> &plan);
+
 /// Whether the placement is one device's whole row in order (no gather needed).
 bool placement_is_identity(const DevicePlacement &pl, int n_station);
 

@@ -9,7 +9,7 @@
 // accumulator), issued as packed FP32x2 instructions.
 //
 // Shape: a CTA owns a tile of 32 channels (lane = channel) and a group of 4x4
-// station blocks (warp = block pair). Spectra for 4 to 12 frames of every
+// station blocks (warp = block pair). Spectra for 2 to 12 frames of every
 // station in the tile are staged in shared memory by a 3-deep cp.async ring;
 // each thread keeps 16 complex accumulators in registers for the whole launch
 // and adds them into the row once at the end. Unlike the reference (one thread
@@ -27,10 +27,10 @@ namespace {
 
 constexpr int kXch = 32;     // channels per CTA, one per lane
 constexpr int kXstages = 3;  // cp.async ring depth
-// frames per pipeline stage: as many of 12, 8, 4 as three stages fit in shared
-// memory (12 up to 24 padded stations, 8 up to 36); fewer stages mean fewer
-// CTA barriers
-constexpr int kXfsWidest = 12, kXfsWide = 8, kXfsNarrow = 4;
+// frames per pipeline stage: as many of 12, 8, 4, 2 as three stages fit in
+// shared memory (12 up to 24 padded stations, 8 up to 36, 4 up to 72, 2 up to
+// 144); fewer stages mean fewer CTA barriers
+constexpr int kXfsWidest = 12, kXfsWide = 8, kXfsNarrow = 4, kXfsTiny = 2;
 constexpr int kBlk = 4;      // stations per block
 
 __device__ __forceinline__ void decode_pair(int p, int nb, int *bj, int *bk) {
@@ -280,12 +280,16 @@ corr_status xengine_plain_launch(const XengineArgs &a, int num_sms, cudaStream_t
     const size_t per_frame = static_cast<size_t>(kXstages) * npad * kXch * sizeof(float2);
     const int fs = per_frame * kXfsWidest <= 227 * 1024 ? kXfsWidest
                  : per_frame * kXfsWide <= 227 * 1024   ? kXfsWide
-                                                        : kXfsNarrow;
+                 : per_frame * kXfsNarrow <= 227 * 1024 ? kXfsNarrow
+                                                        : kXfsTiny;
+    if (per_frame * fs > 227 * 1024)
+        return failf(CORR_ERR_ARG, "plain X-engine: %d stations do not fit in shared memory",
+                     a.n_station);
     const size_t smem = per_frame * fs;
     static PerDevice setup;   // the shared-memory limit is a per-device setting
     corr_status st = setup.run([](int) {
         for (auto k : {xengine_plain_kernel<kXfsWidest>, xengine_plain_kernel<kXfsWide>,
-                       xengine_plain_kernel<kXfsNarrow>}) {
+                       xengine_plain_kernel<kXfsNarrow>, xengine_plain_kernel<kXfsTiny>}) {
             corr_status s2 =
                 cuda_check(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 227 * 1024),
@@ -298,7 +302,8 @@ corr_status xengine_plain_launch(const XengineArgs &a, int num_sms, cudaStream_t
     dim3 grid(groups, a.n_freq / kXch);
     auto k = fs == kXfsWidest ? xengine_plain_kernel<kXfsWidest>
            : fs == kXfsWide   ? xengine_plain_kernel<kXfsWide>
-                              : xengine_plain_kernel<kXfsNarrow>;
+           : fs == kXfsNarrow ? xengine_plain_kernel<kXfsNarrow>
+                              : xengine_plain_kernel<kXfsTiny>;
     k<<<grid, per_cta * 32, smem, stream>>>(a.y, a.y_frames, a.ytile, a.n_station, npad,
                                             a.n_freq, a.frames, a.acc, a.acc64, per_cta,
                                             n_pairs);

@@ -80,7 +80,11 @@ typedef enum corr_status {
  * Checked by corr_create():
  *   abi_version == CORR_ABI_VERSION and struct_size == sizeof(corr_config)
  *                                              (else CORR_ERR_ABI)
- *   n_station >= 1 and n_station*(n_station+1)/2 <= 1024
+ *   1 <= n_station <= 128, and every configured device owns at most 1024
+ *       baselines under the split (the reference's per-device limit,
+ *       corr-cuda/src/kernels.cu:474-483): n_station <= 44 on one device or
+ *       under the time slice (every device owns every baseline); more stations
+ *       when the baseline range or pair covering split them over devices
  *   n_freq a multiple of 2048 up to 32768, as the reference requires (a
  *       frame must be whole 4096-sample packets), or 512 or 1024 (the engine
  *       only needs a transform length it has a plan for). Multiples of 2048

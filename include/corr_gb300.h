@@ -34,7 +34,7 @@ corr_status corr_set_xengine(void *ctx, int32_t mode);
 
 typedef struct corrx_params {
     uint32_t struct_size; /* sizeof(corrx_params)                                 */
-    int32_t  n_station;   /* 1..44                                                */
+    int32_t  n_station;   /* 1..128 (the tensor X-engines: 1..64)                 */
     int32_t  n_freq;      /* 512, 1024, or a multiple of 2048 up to 32768          */
     int32_t  max_frames;  /* frames per F/X pass; sizes the spectra buffer
                              (max_frames*n_station*n_freq*8 bytes)               */

@@ -223,3 +223,24 @@ def test_two_physical_devices_in_one_process(pkg, cuda, frames, one_device):
     from the first call on each."""
     got = run(pkg, frames, 2, SLICE)
     assert got.tobytes() == one_device.tobytes()
+
+
+@pytest.mark.parametrize("split,n_dev", [(RANGE, 2), (COVER, 3)])
+def test_more_than_44_stations_split_over_devices(pkg, shared_gpu, oracle, split, n_dev):
+    """The reference limits baselines per device (corr-cuda/src/kernels.cu:474-483):
+    50 stations (1275 baselines) are accepted once the split leaves every device
+    at most 1024, and give the oracle's rows; the time slice, which gives every
+    device every baseline, is refused."""
+    n, nf, n_cum, fps = 50, 2048, 32, 32
+    rng = np.random.default_rng(5000 + split)
+    x = rng.integers(-30, 31, size=(1, n, n_cum, 2 * nf), dtype=np.int8)
+    plans = []
+    got = drive_rows(pkg, x, n_cum, fps, chunk_frames=16, block_slots=3, rows_per_fetch=1,
+                     devices=list(range(n_dev)), split_mode=split, plans=plans)
+    assert max(p["n_baseline"] for p in plans) <= 1024
+    ref = oracle.correlate_rows(x, n_cum)
+    assert oracle.rel_rms(got, ref) < 1e-5
+    assert oracle.normalized_max_err(got, ref, n) < 1e-5
+    cfg = pkg.make_config(n, nf, fps, 16, 3, 1, split_mode=SLICE, devices=[0, 1])
+    ctx = C.c_void_p()
+    assert pkg.abi.load().corr_create(C.byref(cfg), C.byref(ctx)) == pkg.abi.CORR_ERR_ARG

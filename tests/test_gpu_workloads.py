@@ -126,6 +126,32 @@ def test_abi_at_multiples_of_2048(pkg, cuda, oracle, n_freq):
             assert oracle.normalized_max_err(got, ref, n) < PER_VIS_TOL
 
 
+@pytest.mark.parametrize("n", [64, 100, 128])
+def test_many_stations_on_one_engine(pkg, cuda, oracle, n):
+    """The plain X-engine up to 128 stations (two-frame shared-memory stages from
+    73 padded stations); the tensor forms stop at 64 with CORR_ERR_NOT_IMPL."""
+    torch = cuda
+    nf, frames = 1024, 7
+    rng = np.random.default_rng(n)
+    x = rng.integers(-40, 41, size=(n, frames, 2 * nf)).astype(np.int8)
+    eng = pkg.FxEngine(n, nf, max_frames=8)
+    try:
+        acc = eng.new_acc()
+        eng.accumulate(torch.from_numpy(x).cuda(), frames, acc)
+        torch.cuda.synchronize()
+        eng.check()
+        ref = oracle.correlate(x)
+        got = acc.cpu().numpy()
+        assert oracle.rel_rms(got, ref) < REL_RMS_TOL
+        assert oracle.normalized_max_err(got, ref, n) < PER_VIS_TOL
+    finally:
+        eng.close()
+    if n > 64:
+        with pytest.raises(pkg.abi.CorrError) as e:
+            pkg.FxEngine(n, nf, max_frames=8, xmode=1)
+        assert e.value.status == pkg.abi.CORR_ERR_NOT_IMPL
+
+
 def test_extreme_samples(pkg, cuda, oracle):
     """Full-scale int8 (+127/-128 square waves, impulses): sign handling and range."""
     torch = cuda

@@ -153,3 +153,39 @@ def test_checker_catches_planted_mistakes(pkg):
         p["device_id"] = d
     with pytest.raises(AssertionError):   # ranges out of order
         check_plan(8, 3, SPLITS["range"], rng_plans)
+
+
+@pytest.mark.parametrize("n,nd,split,ok", [
+    (44, 1, "range", True),            # 990 baselines on one device
+    (45, 1, "range", False),           # 1035 > 1024 on one device
+    (45, 2, "range", True),            # 518 + 517
+    (45, 2, "time_slice", False),      # every device owns every baseline
+    (64, 3, "covering", True),         # about 2080 / 3 each
+    (90, 4, "range", True),            # 4095 baselines: 1024, 1024, 1024, 1023
+    (91, 4, "range", False),           # 4186: 1047 on a device
+    (127, 8, "range", True),           # 8128: 1016 each
+    (128, 8, "range", False),          # 8256: 1032 each
+])
+def test_per_device_baseline_limit(pkg, n, nd, split, ok):
+    """The reference's limit is per device (corr-cuda/src/kernels.cu:474-483): at
+    most 1024 baselines owned by any device, so more than 44 stations need their
+    baselines split over several devices."""
+    cfg = pkg.make_config(n, 2048, 32, 32, 2, 1, split_mode=SPLITS[split],
+                          devices=list(range(nd)))
+    if ok:
+        plans = [pkg.plan_query(cfg, d) for d in range(nd)]
+        assert max(p["n_baseline"] for p in plans) <= 1024
+        check_plan(n, nd, SPLITS[split], plans)
+    else:
+        with pytest.raises(pkg.abi.CorrError) as e:
+            pkg.plan_query(cfg, 0)
+        assert e.value.status == pkg.abi.CORR_ERR_ARG
+        assert "per device" in e.value.message
+
+
+def test_station_limit(pkg):
+    cfg = pkg.make_config(129, 2048, 32, 32, 2, 1, split_mode=SPLITS["range"],
+                          devices=list(range(8)))
+    with pytest.raises(pkg.abi.CorrError) as e:
+        pkg.plan_query(cfg, 0)
+    assert "128" in e.value.message
