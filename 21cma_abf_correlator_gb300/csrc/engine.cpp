@@ -191,6 +191,8 @@ corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_s
         xa.acc = acc;
         xa.acc64 = p->acc64;
         xa.err = p->d_err;
+        xa.pair_first = p->xpair_first;
+        xa.pair_count = p->xpair_count;
         if (p->xmode == CORR_X_PLAIN_FP32)
             st = xengine_plain_launch(xa, p->num_sms, stream);
         else
@@ -389,6 +391,8 @@ extern "C" corr_status corrx_run_xengine(void *eng, int32_t frames, void *d_acc,
     xa.acc = d_acc;
     xa.acc64 = p->acc64;
     xa.err = p->d_err;
+    xa.pair_first = p->xpair_first;
+    xa.pair_count = p->xpair_count;
     if (p->xmode == CORR_X_PLAIN_FP32)
         return xengine_plain_launch(xa, p->num_sms, static_cast<cudaStream_t>(stream));
     return xengine_tc_launch(xa, p->xmode == CORR_X_TC_FP16_SPLIT, p->xct, p->xkt, p->num_sms,
@@ -400,6 +404,19 @@ extern "C" corr_status corrx_run_xengine(void *eng, int32_t frames, void *d_acc,
 // ---------------------------------------------------------------------------
 
 namespace corrgb {
+
+void fxplan_limit_baselines(FxPlan *p, int first, int count) {
+    p->xpair_first = p->xpair_count = 0;
+    const int n = p->n_station, nb = n * (n + 1) / 2;
+    if (count <= 0 || first < 0 || first + count > nb || count == nb) return;
+    auto row_of = [n](int b) {   // first station of baseline b (row-major, j <= k)
+        int j = 0;
+        while (b >= n - j) b -= n - j++;
+        return j;
+    };
+    xengine_plain_pair_span(n, row_of(first), row_of(first + count - 1), &p->xpair_first,
+                            &p->xpair_count);
+}
 
 corr_status fxplan_set_tiles(FxPlan *p, int ytile, int xct, int xkt, int fplan) {
     if (fplan < 0 || fplan >= fengine_plans(p->n_freq))

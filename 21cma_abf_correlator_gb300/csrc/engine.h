@@ -168,6 +168,10 @@ struct XengineArgs {
     void *acc;                  // acc[b*n_freq + c] += (float2, or double2 if acc64)
     int acc64;
     int *err;
+    // plain X-engine: compute only the station-block pairs [pair_first,
+    // pair_first + pair_count) of its row-major enumeration (pair_count 0: all)
+    int pair_first;
+    int pair_count;
 };
 
 // fengine.cu
@@ -200,6 +204,10 @@ corr_status fengine_launch(int n_freq, const TwiddleTables &tw, const FengineArg
 
 // xengine.cu
 corr_status xengine_plain_launch(const XengineArgs &a, int num_sms, cudaStream_t stream);
+/// The plain X-engine's station-block pairs that cover the baselines of rows
+/// (first station) row_first .. row_last: a contiguous range of its enumeration.
+void xengine_plain_pair_span(int n_station, int row_first, int row_last, int *pair_first,
+                             int *pair_count);
 corr_status scale_launch(float2 *acc, size_t n, float s, cudaStream_t stream);
 /// acc[i] *= s in double precision over n complex128 values.
 corr_status scale64_launch(double2 *acc, size_t n, double s, cudaStream_t stream);
@@ -240,6 +248,8 @@ struct FxPlan {
     int fplan = 0;        // F-engine FFT radix plan
     int xmode = CORR_X_PLAIN_FP32;
     int acc64 = 0;        // rows are complex128 (CORRX_ACC_FP64) instead of complex64
+    int xpair_first = 0;  // plain X-engine: block pairs to compute (xpair_count 0: all)
+    int xpair_count = 0;
     int num_sms = 0;
     float2 *d_y = nullptr;
     int *d_err = nullptr;
@@ -250,6 +260,11 @@ corr_status fxplan_create(int device, int n_station, int n_freq, int max_frames,
                           FxPlan **out);
 void fxplan_destroy(FxPlan *p);
 corr_status fxplan_set_tiles(FxPlan *p, int ytile, int xct, int xkt, int fplan);
+/// The plain X-engine computes only what the baselines [first, first + count)
+/// of the row-major numbering need (the block pairs of their rows); the other
+/// baselines of the row are left as they are. A device of a baseline-range split
+/// owns such a range. The tensor forms compute every pair regardless.
+void fxplan_limit_baselines(FxPlan *p, int first, int count);
 corr_status fxplan_autotune(FxPlan *p, cudaStream_t stream, corrx_tiles *out);
 
 /// F then X over `frames` frames, in passes of at most max_frames.
