@@ -283,11 +283,20 @@ corr_status xengine_plain_launch(const XengineArgs &a, int num_sms, cudaStream_t
     const int groups = (n_pairs + 31) / 32;
     const int per_cta = (n_pairs + groups - 1) / groups;
     const size_t per_frame = static_cast<size_t>(kXstages) * npad * kXch * sizeof(float2);
-    const int fs = per_frame * kXfsWidest <= 227 * 1024 ? kXfsWidest
-                 : per_frame * kXfsWide <= 227 * 1024   ? kXfsWide
-                 : per_frame * kXfsNarrow <= 227 * 1024 ? kXfsNarrow
-                                                        : kXfsTiny;
-    if (per_frame * fs > 227 * 1024)
+    // Deeper stages mean fewer CTA barriers, but a CTA of few warps (as when only
+    // some block pairs are computed) needs others beside it on its SM: take the
+    // deepest stages among those that give an SM the most warps, up to 16.
+    int fs = 0, best = -1;
+    for (int f : {kXfsWidest, kXfsWide, kXfsNarrow, kXfsTiny}) {
+        const size_t bytes = per_frame * f;
+        if (bytes > 227 * 1024) continue;
+        const int warps = std::min(16, static_cast<int>((227 * 1024) / bytes) * per_cta);
+        if (warps > best) {
+            best = warps;
+            fs = f;
+        }
+    }
+    if (fs == 0 || per_frame * fs > 227 * 1024)
         return failf(CORR_ERR_ARG, "plain X-engine: %d stations do not fit in shared memory",
                      a.n_station);
     const size_t smem = per_frame * fs;
