@@ -194,3 +194,37 @@ def test_callbacks(pkg, cuda):
         assert wait_for(6)
         assert lib.corr_rows_fetch_ready(ctx) == OK
         assert np.abs(out).max() > 0
+
+
+def test_contexts_leave_no_device_memory_behind(pkg, cuda):
+    """Creating and destroying contexts over and over (one device, and four
+    configured devices of each split on the one GPU) returns every device byte:
+    free memory after twelve cycles is what it was after the first."""
+    torch = cuda
+
+    def cycle(devices, split):
+        if len(devices) > 1:
+            pkg.set_device_map([0] * len(devices))
+        try:
+            cfg = pkg.make_config(8, 4096, 64, 32, 3, 2, split_mode=split, devices=devices)
+            with pkg.Correlator(cfg) as c:
+                for g in range(8):
+                    c.staging(g).mask[0, :] = 0xFF
+                c.row_accumulate(0, 64)
+                c.row_end(64)
+                c.rows_wait()
+                c.rows_fetch()
+                c.row_slot_free(0)
+        finally:
+            pkg.set_device_map(None)
+        torch.cuda.synchronize()
+
+    forms = [([0], 0), ([0, 1, 2, 3], 0), ([0, 1, 2, 3], 1), ([0, 1, 2, 3], 2)]
+    for d, s in forms:            # first use: kernel modules and per-device set-up
+        cycle(d, s)
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        for d, s in forms:
+            cycle(d, s)
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free0 - free1 < 8 << 20, f"{(free0 - free1) >> 20} MiB not returned"
