@@ -968,12 +968,14 @@ def run_e2e(pkg, w, x, mask, xmode, args, torch) -> dict:
         v.samples[:] = host[g].reshape(block_slots, fps, L)
     out = np.empty(c.fetch_bytes() // 8, dtype=np.complex64)
     import ctypes as C
-    pinned = C.c_void_p()
-    pkg.abi.check(c.lib.corr_host_alloc(out.nbytes, C.byref(pinned)), "corr_host_alloc")
+    pinned = [C.c_void_p(), C.c_void_p()]
+    for buf in pinned:
+        pkg.abi.check(c.lib.corr_host_alloc(out.nbytes, C.byref(buf)), "corr_host_alloc")
     rows = C.c_int32()
     seq = [0]
+    done = pkg.abi.NOTIFY_FN(lambda _user: None)
 
-    def integration():
+    def integration(i, blocking):
         for f0 in range(0, F, fps):
             s = seq[0]
             if s >= block_slots:
@@ -983,24 +985,41 @@ def run_e2e(pkg, w, x, mask, xmode, args, torch) -> dict:
             c.row_accumulate(s, min(fps, F - f0))
             seq[0] += 1
         c.row_end(F)
-        pkg.abi.check(c.lib.corr_rows_fetch(c.ctx, pinned, out.nbytes, C.byref(rows)),
-                      "corr_rows_fetch")
+        if blocking:
+            pkg.abi.check(c.lib.corr_rows_fetch(c.ctx, pinned[0], out.nbytes, C.byref(rows)),
+                          "corr_rows_fetch")
+        else:
+            # the row's fetch is queued and the next integration's copies start
+            # at once; two pinned buffers alternate
+            pkg.abi.check(c.lib.corr_rows_fetch_submit(c.ctx, pinned[i % 2], out.nbytes,
+                                                       C.byref(rows), done, None),
+                          "corr_rows_fetch_submit")
 
-    for _ in range(2):
-        integration()
+    def wait_fetches():
+        while c.lib.corr_rows_fetch_ready(c.ctx) == pkg.abi.CORR_ERR_BUSY:
+            time.sleep(20e-6)
+
     # wall clock on the host: the median of three rounds, so that one hiccup of
     # the host's scheduler does not stand for the path
     k = max(2, args.steps // 2)
-    rounds = []
-    for _ in range(3):
-        t0 = time.perf_counter()
-        for _ in range(k):
-            integration()
-        rounds.append((time.perf_counter() - t0) / k)
-    dt = statistics.median(rounds)
+    medians = {}
+    for blocking in (True, False):
+        for i in range(2):
+            integration(i, blocking)
+        wait_fetches()
+        rounds = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            for i in range(k):
+                integration(i, blocking)
+            wait_fetches()     # the last row is in host memory
+            rounds.append((time.perf_counter() - t0) / k)
+        medians[blocking] = (statistics.median(rounds), rounds)
+    dt, rounds = medians[False]
     for s in range(seq[0] - 1, max(seq[0] - block_slots, 0) - 1, -1):
         c.row_slot_free(s)
-    c.lib.corr_host_free(pinned)
+    for buf in pinned:
+        c.lib.corr_host_free(buf)
     c.close()
     mb = (fps + 7) // 8
     h2d = N * F * L + N * mb * (F // fps)
@@ -1008,7 +1027,12 @@ def run_e2e(pkg, w, x, mask, xmode, args, torch) -> dict:
     return {"value": N * F * L / dt / 1e9, "unit": "GSample/s", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "ms_per_step": dt * 1e3, "steps": k,
             "rounds_ms": [r * 1e3 for r in rounds],
-            "path": "corr_row_accumulate/row_end/rows_fetch from pinned staging",
+            "path": "corr_row_accumulate/row_end/rows_fetch_submit from pinned staging: each "
+                    "row's fetch overlaps the next integration's copies",
+            "blocking_fetch": {"value": N * F * L / medians[True][0] / 1e9,
+                               "ms_per_step": medians[True][0] * 1e3,
+                               "path": "the same with corr_rows_fetch, one integration after "
+                                       "the other"},
             "tiles": tiles}
 
 
