@@ -953,10 +953,11 @@ def run_writer(pkg, w, n_rows: int = 8) -> dict:
 def run_e2e(pkg, w, x, mask, xmode, args, torch) -> dict:
     """The integration through the C ABI: staging -> H2D -> F+X -> row -> host."""
     N, L, F = w.n_station, w.fft_len, w.frames
-    # 256-frame slots in a 4-slot ring; smaller for short integrations (the ring
-    # is filled once from the integration's own frames)
+    # 256-frame slots in an 8-slot ring, as the shipped configuration has them
+    # (config/correlator.yaml: frames_per_slot 256, block_slots 8); fewer for short
+    # integrations (the ring is filled once from the integration's own frames)
     fps = min(256, max(1, F // 2))
-    block_slots = max(2, min(4, F // fps))
+    block_slots = max(2, min(8, F // fps))
     cfg = pkg.make_config(N, w.n_freq, fps, fps, block_slots, 1)
     c = pkg.Correlator(cfg)
     c.set_xengine(xmode)
