@@ -570,11 +570,11 @@ corr_status build_share(Context *c, Share &s, int home_physical) {
                             &s.plan)) != CORR_OK)
         return st;
     s.plan->acc64 = 1;
-    // A device of a baseline-range split owns one contiguous range of the
-    // baselines of its (all) stations: the plain X-engine computes only what that
-    // range needs, so the devices divide the X-engine's work.
-    if (c->cfg.split_mode == CORR_SPLIT_BASELINE_RANGE && s.pl.contiguous && !s.pl.local.empty())
-        fxplan_limit_baselines(s.plan, s.pl.local.front(), static_cast<int>(s.pl.local.size()));
+    // A device of the baseline-range or pair-covering split owns only some
+    // baselines of its stations' matrix: the plain X-engine computes only the
+    // station-block pairs that hold them, so the devices divide its work.
+    if (!c->time_slice && (st = fxplan_limit_baselines(s.plan, s.pl.local)) != CORR_OK)
+        return st;
     s.ring_station_stride = static_cast<size_t>(cfg.chunk_frames) * c->lay.frame_stride;
     s.row_elems = static_cast<size_t>(n * (n + 1) / 2) * static_cast<size_t>(cfg.n_freq);
     const size_t ring_bytes = s.ring_station_stride * static_cast<size_t>(n);

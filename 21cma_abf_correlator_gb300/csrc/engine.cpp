@@ -9,6 +9,7 @@
 // (corr-cuda/src/kernels.cu:806-845), minus the host copies, which belong to the
 // caller (abi.cpp for the staging ring).
 
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -141,6 +142,7 @@ void fxplan_destroy(FxPlan *p) {
     fengine_release(&p->tw);
     if (p->d_y) cudaFree(p->d_y);
     if (p->d_err) cudaFree(p->d_err);
+    if (p->d_xpair_list) cudaFree(p->d_xpair_list);
     delete p;
 }
 
@@ -193,6 +195,7 @@ corr_status fxplan_accumulate(FxPlan *p, const int8_t *samples, size_t station_s
         xa.err = p->d_err;
         xa.pair_first = p->xpair_first;
         xa.pair_count = p->xpair_count;
+        xa.pair_list = p->d_xpair_list;
         if (p->xmode == CORR_X_PLAIN_FP32)
             st = xengine_plain_launch(xa, p->num_sms, stream);
         else
@@ -393,6 +396,7 @@ extern "C" corr_status corrx_run_xengine(void *eng, int32_t frames, void *d_acc,
     xa.err = p->d_err;
     xa.pair_first = p->xpair_first;
     xa.pair_count = p->xpair_count;
+    xa.pair_list = p->d_xpair_list;
     if (p->xmode == CORR_X_PLAIN_FP32)
         return xengine_plain_launch(xa, p->num_sms, static_cast<cudaStream_t>(stream));
     return xengine_tc_launch(xa, p->xmode == CORR_X_TC_FP16_SPLIT, p->xct, p->xkt, p->num_sms,
@@ -405,17 +409,44 @@ extern "C" corr_status corrx_run_xengine(void *eng, int32_t frames, void *d_acc,
 
 namespace corrgb {
 
-void fxplan_limit_baselines(FxPlan *p, int first, int count) {
+corr_status fxplan_limit_baselines(FxPlan *p, const std::vector<int32_t> &baselines) {
     p->xpair_first = p->xpair_count = 0;
+    if (p->d_xpair_list != nullptr) {
+        cudaSetDevice(p->device);
+        cudaFree(p->d_xpair_list);
+        p->d_xpair_list = nullptr;
+    }
     const int n = p->n_station, nb = n * (n + 1) / 2;
-    if (count <= 0 || first < 0 || first + count > nb || count == nb) return;
-    auto row_of = [n](int b) {   // first station of baseline b (row-major, j <= k)
-        int j = 0;
-        while (b >= n - j) b -= n - j++;
-        return j;
-    };
-    xengine_plain_pair_span(n, row_of(first), row_of(first + count - 1), &p->xpair_first,
-                            &p->xpair_count);
+    if (baselines.empty() || static_cast<int>(baselines.size()) == nb) return CORR_OK;
+    // the block pair of each baseline (row-major over j <= k), in order, once
+    std::vector<int> row_start(static_cast<size_t>(n) + 1, 0);
+    for (int j = 0; j < n; ++j) row_start[static_cast<size_t>(j) + 1] = row_start[j] + (n - j);
+    std::vector<int32_t> pairs;
+    for (int32_t g : baselines) {
+        if (g < 0 || g >= nb) return failf(CORR_ERR_INTERNAL, "baseline %d outside the row", g);
+        const int j = static_cast<int>(std::upper_bound(row_start.begin(), row_start.end(), g) -
+                                       row_start.begin()) - 1;
+        const int k = j + (g - row_start[static_cast<size_t>(j)]);
+        pairs.push_back(xengine_plain_block_pair(n, j, k));
+    }
+    std::sort(pairs.begin(), pairs.end());
+    pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
+    const int count = static_cast<int>(pairs.size());
+    if (pairs.back() - pairs.front() + 1 == count) {   // a contiguous run: first and count
+        p->xpair_first = pairs.front();
+        p->xpair_count = count;
+        return CORR_OK;
+    }
+    corr_status st = cuda_check(cudaSetDevice(p->device), "cudaSetDevice");
+    if (st != CORR_OK) return st;
+    const size_t bytes = pairs.size() * sizeof(int32_t);
+    if ((st = cuda_check(cudaMalloc(&p->d_xpair_list, bytes), "cudaMalloc(block pairs)")) !=
+            CORR_OK ||
+        (st = cuda_check(cudaMemcpy(p->d_xpair_list, pairs.data(), bytes, cudaMemcpyHostToDevice),
+                         "cudaMemcpy(block pairs)")) != CORR_OK)
+        return st;
+    p->xpair_count = count;
+    return CORR_OK;
 }
 
 corr_status fxplan_set_tiles(FxPlan *p, int ytile, int xct, int xkt, int fplan) {

@@ -169,9 +169,11 @@ struct XengineArgs {
     int acc64;
     int *err;
     // plain X-engine: compute only the station-block pairs [pair_first,
-    // pair_first + pair_count) of its row-major enumeration (pair_count 0: all)
+    // pair_first + pair_count) of its row-major enumeration (pair_count 0: all),
+    // or, with pair_list, the pair_count pairs it names
     int pair_first;
     int pair_count;
+    const int32_t *pair_list;
 };
 
 // fengine.cu
@@ -204,10 +206,9 @@ corr_status fengine_launch(int n_freq, const TwiddleTables &tw, const FengineArg
 
 // xengine.cu
 corr_status xengine_plain_launch(const XengineArgs &a, int num_sms, cudaStream_t stream);
-/// The plain X-engine's station-block pairs that cover the baselines of rows
-/// (first station) row_first .. row_last: a contiguous range of its enumeration.
-void xengine_plain_pair_span(int n_station, int row_first, int row_last, int *pair_first,
-                             int *pair_count);
+/// The plain X-engine's station-block pair holding baseline (j, k), j <= k: its
+/// index in the row-major enumeration of block pairs.
+int xengine_plain_block_pair(int n_station, int j, int k);
 corr_status scale_launch(float2 *acc, size_t n, float s, cudaStream_t stream);
 /// acc[i] *= s in double precision over n complex128 values.
 corr_status scale64_launch(double2 *acc, size_t n, double s, cudaStream_t stream);
@@ -250,6 +251,7 @@ struct FxPlan {
     int acc64 = 0;        // rows are complex128 (CORRX_ACC_FP64) instead of complex64
     int xpair_first = 0;  // plain X-engine: block pairs to compute (xpair_count 0: all)
     int xpair_count = 0;
+    int32_t *d_xpair_list = nullptr;   // ... or the list of them (device memory)
     int num_sms = 0;
     float2 *d_y = nullptr;
     int *d_err = nullptr;
@@ -260,11 +262,12 @@ corr_status fxplan_create(int device, int n_station, int n_freq, int max_frames,
                           FxPlan **out);
 void fxplan_destroy(FxPlan *p);
 corr_status fxplan_set_tiles(FxPlan *p, int ytile, int xct, int xkt, int fplan);
-/// The plain X-engine computes only what the baselines [first, first + count)
-/// of the row-major numbering need (the block pairs of their rows); the other
-/// baselines of the row are left as they are. A device of a baseline-range split
-/// owns such a range. The tensor forms compute every pair regardless.
-void fxplan_limit_baselines(FxPlan *p, int first, int count);
+/// The plain X-engine computes only the station-block pairs that hold the given
+/// baselines (indices of the row-major numbering over the plan's stations); the
+/// other baselines of the row are left as they are. A device of a baseline-range
+/// split owns a contiguous range of them, one of pair covering a scattered set.
+/// The tensor forms compute every pair regardless.
+corr_status fxplan_limit_baselines(FxPlan *p, const std::vector<int32_t> &baselines);
 corr_status fxplan_autotune(FxPlan *p, cudaStream_t stream, corrx_tiles *out);
 
 /// F then X over `frames` frames, in passes of at most max_frames.

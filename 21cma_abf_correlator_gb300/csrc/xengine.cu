@@ -47,7 +47,8 @@ template <int kXfs>
 __global__ void __launch_bounds__(1024, 1)
     xengine_plain_kernel(const float2 *__restrict__ y, int y_frames, int ytile, int n_station,
                          int npad, int n_freq, int frames, void *__restrict__ acc,
-                         int acc64, int pairs_per_cta, int pair_first, int n_pairs) {
+                         int acc64, int pairs_per_cta, int pair_first, int n_pairs,
+                         const int32_t *__restrict__ pair_list) {
     extern __shared__ __align__(16) float2 xs[];   // [stage][frame][npad][32]
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -55,8 +56,8 @@ __global__ void __launch_bounds__(1024, 1)
     const int c0 = blockIdx.y * kXch;
     const int nb = npad / kBlk;
     const int q = blockIdx.x * pairs_per_cta + warp;   // among the pairs computed
-    const int p = pair_first + q;
     const bool active = q < n_pairs && warp < pairs_per_cta;
+    const int p = !active ? 0 : pair_list != nullptr ? pair_list[q] : pair_first + q;
     int bj = 0, bk = 0;
     if (active) decode_pair(p, nb, &bj, &bk);
 
@@ -276,9 +277,10 @@ corr_status xengine_plain_launch(const XengineArgs &a, int num_sms, cudaStream_t
     const int npad = (a.n_station + kBlk - 1) / kBlk * kBlk;
     const int nb = npad / kBlk;
     const int all_pairs = nb * (nb + 1) / 2;
-    const bool part = a.pair_count > 0 && a.pair_first >= 0 &&
-                      a.pair_first + a.pair_count <= all_pairs;
-    const int pair_first = part ? a.pair_first : 0;
+    const bool list = a.pair_list != nullptr && a.pair_count > 0 && a.pair_count <= all_pairs;
+    const bool part = list || (a.pair_count > 0 && a.pair_first >= 0 &&
+                               a.pair_first + a.pair_count <= all_pairs);
+    const int pair_first = part && !list ? a.pair_first : 0;
     const int n_pairs = part ? a.pair_count : all_pairs;
     const int groups = (n_pairs + 31) / 32;
     const int per_cta = (n_pairs + groups - 1) / groups;
@@ -320,18 +322,15 @@ corr_status xengine_plain_launch(const XengineArgs &a, int num_sms, cudaStream_t
                               : xengine_plain_kernel<kXfsTiny>;
     k<<<grid, per_cta * 32, smem, stream>>>(a.y, a.y_frames, a.ytile, a.n_station, npad,
                                             a.n_freq, a.frames, a.acc, a.acc64, per_cta,
-                                            pair_first, n_pairs);
+                                            pair_first, n_pairs, list ? a.pair_list : nullptr);
     return cuda_check(cudaGetLastError(), "xengine_plain_kernel launch");
 }
 
-void xengine_plain_pair_span(int n_station, int row_first, int row_last, int *pair_first,
-                             int *pair_count) {
+int xengine_plain_block_pair(int n_station, int j, int k) {
     const int nb = (n_station + kBlk - 1) / kBlk;
-    // block pairs (bj, bk), bj <= bk, row-major: index bj*nb - bj*(bj-1)/2 + (bk - bj)
-    auto index = [nb](int bj, int bk) { return bj * nb - bj * (bj - 1) / 2 + (bk - bj); };
-    const int bj0 = row_first / kBlk, bj1 = row_last / kBlk;
-    *pair_first = index(bj0, bj0);
-    *pair_count = index(bj1, nb - 1) - *pair_first + 1;
+    const int bj = j / kBlk, bk = k / kBlk;
+    // block pairs (bj, bk), bj <= bk, row-major
+    return bj * nb - bj * (bj - 1) / 2 + (bk - bj);
 }
 
 corr_status scale_launch(float2 *acc, size_t n, float s, cudaStream_t stream) {
