@@ -53,13 +53,23 @@ struct Dft<2> {
 
 template <>
 struct Dft<4> {
-    static __device__ __forceinline__ void run(float2 *v) {
-        const float2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
-        const float2 s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
+    static __device__ __forceinline__ void finish(float2 s02, float2 d02, float2 s13, float2 d13,
+                                                  float2 *v) {
         v[0] = cadd(s02, s13);
         v[2] = csub(s02, s13);
         v[1] = make_float2(d02.x + d13.y, d02.y - d13.x); // d02 - i*d13
         v[3] = make_float2(d02.x - d13.y, d02.y + d13.x); // d02 + i*d13
+    }
+    static __device__ __forceinline__ void run(float2 *v) {
+        finish(cadd(v[0], v[2]), csub(v[0], v[2]), cadd(v[1], v[3]), csub(v[1], v[3]), v);
+    }
+    // Inputs still carrying the int8 unpacking's offset B (x[n] = b[n] + B, every
+    // value an integer below 2^24): x0 - x2 = b0 - b2 and x0 + (x2 - 2B) = b0 + b2
+    // exactly, so the offset goes in one subtraction per pair instead of one per
+    // input, with the same results as run() on b.
+    static __device__ __forceinline__ void run_biased(float2 *v, float2 two_b) {
+        finish(cadd(v[0], csub(v[2], two_b)), csub(v[0], v[2]), cadd(v[1], csub(v[3], two_b)),
+               csub(v[1], v[3]), v);
     }
 };
 
@@ -112,19 +122,23 @@ __host__ __device__ constexpr float sin_odd(int R, int m) {
 // s_n = x[n] + x[R-n] and d_n = x[n] - x[R-n] (n = 1..H, H = (R-1)/2)
 //   X[k]   = x[0] + sum_n s_n cos(2*pi*n*k/R) - i sum_n d_n sin(2*pi*n*k/R)
 //   X[R-k] = the same with +i,                     k = 1..H.
+// BIASED: the inputs still carry the int8 unpacking's offset B (every value an
+// integer below 2^24): s_n = x[n] + (x[R-n] - 2B), d_n = x[n] - x[R-n] and
+// x[0] - B are then exact, the same numbers as from the unbiased inputs.
 template <int R>
 struct DftOdd {
     static constexpr int H = (R - 1) / 2;
-    static __device__ __forceinline__ void run(float2 *v) {
+    template <bool BIASED = false>
+    static __device__ __forceinline__ void run(float2 *v, float2 two_b = float2{}) {
         float2 s[H], d[H];
-        float2 sum = v[0];
+        const float2 x0 = BIASED ? csub(v[0], make_float2(0.5f * two_b.x, 0.5f * two_b.y)) : v[0];
+        float2 sum = x0;
 #pragma unroll
         for (int n = 1; n <= H; ++n) {
-            s[n - 1] = cadd(v[n], v[R - n]);
+            s[n - 1] = cadd(v[n], BIASED ? csub(v[R - n], two_b) : v[R - n]);
             d[n - 1] = csub(v[n], v[R - n]);
             sum = cadd(sum, s[n - 1]);
         }
-        const float2 x0 = v[0];
 #pragma unroll
         for (int k = 1; k <= H; ++k) {
             float2 a = x0, b = make_float2(0.f, 0.f);
@@ -177,17 +191,22 @@ struct Dft<15> {
     }
 };
 
-// R = 4 x (R/4): n = (R/4)*n1 + n2, k = k1 + 4*k2.
+// R = 4 x (R/4): n = (R/4)*n1 + n2, k = k1 + 4*k2. BIASED: the inputs still
+// carry the int8 unpacking's offset (Dft<4>::run_biased).
 template <int R>
 struct Dft {
     static_assert(R == 8 || R == 16 || R == 32, "radix");
     static constexpr int R2 = R / 4;
-    static __device__ __forceinline__ void run(float2 *v) {
+    template <bool BIASED = false>
+    static __device__ __forceinline__ void run(float2 *v, float2 two_b = float2{}) {
         float2 b[R2][4];
 #pragma unroll
         for (int n2 = 0; n2 < R2; ++n2) {
             float2 t[4] = {v[n2], v[R2 + n2], v[2 * R2 + n2], v[3 * R2 + n2]};
-            Dft<4>::run(t);
+            if constexpr (BIASED)
+                Dft<4>::run_biased(t, two_b);
+            else
+                Dft<4>::run(t);
 #pragma unroll
             for (int k1 = 0; k1 < 4; ++k1) b[n2][k1] = mul_w32(t[k1], n2 * k1 * (32 / R));
         }
@@ -315,11 +334,15 @@ struct FeCfg {
 // conversion unit: flipping the sign bit gives b + 128 in [0, 255]; placed in the
 // low byte of 0x4B000000 that is the float 2^23 + b + 128, and subtracting
 // 2^23 + 128 leaves b.
-__device__ __forceinline__ float2 int8_pair_to_float2(uint16_t u) {
+constexpr float kInt8Bias = 8388736.0f;   // 2^23 + 128
+__device__ __forceinline__ float2 int8_pair_to_biased(uint16_t u) {
     const uint32_t x = static_cast<uint32_t>(u) ^ 0x8080u;
-    const float lo = __uint_as_float(__byte_perm(x, 0x4B000000u, 0x7440));
-    const float hi = __uint_as_float(__byte_perm(x, 0x4B000000u, 0x7441));
-    return make_float2(lo - 8388736.0f, hi - 8388736.0f);
+    return make_float2(__uint_as_float(__byte_perm(x, 0x4B000000u, 0x7440)),
+                       __uint_as_float(__byte_perm(x, 0x4B000000u, 0x7441)));
+}
+__device__ __forceinline__ float2 int8_pair_to_float2(uint16_t u) {
+    const float2 x = int8_pair_to_biased(u);
+    return make_float2(x.x - kInt8Bias, x.y - kInt8Bias);
 }
 
 // Shared-memory index padding: one float2 per R0 elements, which makes the
@@ -381,21 +404,32 @@ __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *_
     constexpr bool RUNS = NS % (1 << SHIFT) == 0 || (NS == 1 && R == (1 << SHIFT));
     constexpr int PSTRIDE = STRIDE + (STRIDE >> SHIFT);
     constexpr int PNS = (NS == 1) ? 1 : NS + (NS >> SHIFT);
+    // The int8 first pass leaves the unpacking's offset in its inputs; the DFT's
+    // first butterflies take it out (Dft<4>::run_biased, DftOdd).
+    constexpr bool BIASED = SRC == kFromInt8 && (R == 3 || R == 5 || R == 7 || R == 8 ||
+                                                 R == 16 || R == 32);
+    static_assert(!BIASED || (NS == 1 && !TAB), "the biased inputs take no twiddles");
     const uint16_t *x16 = reinterpret_cast<const uint16_t *>(sx);
-    auto compute = [&](int j, float2 *v) {
-        if constexpr (SRC == kFromInt8) {
+    auto gather = [&](int j, float2 *v) {
+        if constexpr (BIASED) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[r] = int8_pair_to_biased(x16[j + r * STRIDE]);
+        } else if constexpr (SRC == kFromInt8) {
 #pragma unroll
             for (int r = 0; r < R; ++r) v[r] = int8_pair_to_float2(x16[j + r * STRIDE]);
         } else if constexpr (SRC == kFromInt8Sum) {
+            // with the offset B still in: x[e] + (x[e+M] - 2B) and x[e] - x[e+M]
+            // are the integer sum and difference, exactly (Dft<4>::run_biased)
+            const float2 two_b = make_float2(2.0f * kInt8Bias, 2.0f * kInt8Bias);
 #pragma unroll
             for (int r = 0; r < R; ++r)
-                v[r] = cadd(int8_pair_to_float2(x16[j + r * STRIDE]),
-                            int8_pair_to_float2(x16[j + r * STRIDE + M]));
+                v[r] = cadd(int8_pair_to_biased(x16[j + r * STRIDE]),
+                            csub(int8_pair_to_biased(x16[j + r * STRIDE + M]), two_b));
         } else if constexpr (SRC == kFromInt8Diff) {
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int e = j + r * STRIDE;
-                v[r] = cmul(csub(int8_pair_to_float2(x16[e]), int8_pair_to_float2(x16[e + M])),
+                v[r] = cmul(csub(int8_pair_to_biased(x16[e]), int8_pair_to_biased(x16[e + M])),
                             cmul(qlo[e & 63], qhi[e >> 6]));
             }
         } else {
@@ -410,7 +444,12 @@ __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *_
         } else if constexpr (NS > 1) {
             apply_twiddles<R>(v, mod_c<NS>(j) * (M / (NS * R)), lo, hi);
         }
-        Dft<R>::run(v);
+    };
+    auto transform = [&](float2 *v) {
+        if constexpr (BIASED)
+            Dft<R>::template run<true>(v, make_float2(2.0f * kInt8Bias, 2.0f * kInt8Bias));
+        else
+            Dft<R>::run(v);
     };
     auto store = [&](int j, const float2 *v) {
         const int base = div_c<NS>(j) * (NS * R) + mod_c<NS>(j);
@@ -430,7 +469,8 @@ __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *_
             const int j = tid + q * T;
             if (!EXACT && j >= STRIDE) continue;
             float2 v[R];
-            compute(j, v);
+            gather(j, v);
+            transform(v);
             store(j, v);
         }
     } else {
@@ -439,7 +479,8 @@ __device__ __forceinline__ void fft_pass(float2 *__restrict__ sd, const char2 *_
         for (int q = 0; q < NB; ++q) {
             const int j = tid + q * T;
             if (!EXACT && j >= STRIDE) continue;
-            compute(j, v[q]);
+            gather(j, v[q]);
+            transform(v[q]);
         }
         __syncthreads();
 #pragma unroll
@@ -483,8 +524,9 @@ __device__ __forceinline__ void last_pass_store(const float2 *__restrict__ sd,
     apply_twiddles<R>(b, j2, plo, phi);
     Dft<R>::run(a);   // a[r] = Z[j1 + r*J]
     Dft<R>::run(b);   // b[r] = Z[j2 + r*J]
-    const float2 w1 = cmul(qlo[j1 & 63], qhi[j1 >> 6]);   // w_{j1}
-    const float2 w2 = cmul(qlo[j2 & 63], qhi[j2 >> 6]);   // w_{j2} (thread 0: w_{J/2})
+    // h*w_{j1} and h*w_{j2} (thread 0: h*w_{J/2}), h = yrow.half (split_store)
+    const float2 w1 = scale_tw(cmul(qlo[j1 & 63], qhi[j1 >> 6]), yrow.half);
+    const float2 w2 = scale_tw(cmul(qlo[j2 & 63], qhi[j2 >> 6]), yrow.half);
     // Second half (i >= H): thread 0 pairs b with itself from k = J/2; the
     // others continue k = j1 + i*J. Both as a base index and a base twiddle
     // chosen once, stepped by compile-time constants.
@@ -537,7 +579,7 @@ __device__ __forceinline__ void last_pass_store_odd(const float2 *__restrict__ s
     apply_twiddles<R>(b, j2, plo, phi);
     Dft<R>::run(a);   // a[r] = B[j1 + r*J]
     Dft<R>::run(b);   // b[r] = B[j2 + r*J]
-    const float2 w1 = cmul(cmul(qlo[j1 & 63], qhi[j1 >> 6]), odd_shift);
+    const float2 w1 = scale_tw(cmul(cmul(qlo[j1 & 63], qhi[j1 >> 6]), odd_shift), yrow.half);
 #pragma unroll
     for (int i = 0; i < R; ++i)   // exp(-pi*i*i/R) = exp(-2*pi*i*i*(16/R)/32)
         split_store(a[i], b[R - 1 - i], mul_w32(w1, i * (16 / R)), j1 + i * J, M - 1, true, yrow);

@@ -491,14 +491,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                 zb[i] = make_float2(__uint_as_float(w[2 * i]), __uint_as_float(w[2 * i + 1]));
             }
             const bool t0 = (p == 0);
-            const float2 wp = tw3[p];
+            const float2 wp = scale_tw(tw3[p], yrow.half);   // split_store takes h*w
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
                 const float2 zmk = t0 ? za[(16 - i) & 15] : zb[15 - i];
                 split_store(za[i], zmk, mul_w32(wp, i), p + 1024 * i, kM, !(t0 && i == 0), yrow);
             }
             const int kB = t0 ? 512 : p + 8192;
-            const float2 wB = t0 ? tw3[512] : mul_w32(wp, 8);
+            const float2 wB = t0 ? scale_tw(tw3[512], yrow.half) : mul_w32(wp, 8);
 #pragma unroll
             for (int i = 8; i < 16; ++i) {
                 const float2 zk = t0 ? zb[i - 8] : za[i];

@@ -90,18 +90,27 @@ struct YRow {
 
 // X[k] = Fe + w_k Fo and X[M-k] = conj(Fe - w_k Fo), with Z = FFT of the packed
 // pairs, Fe = (Z[k] + conj(Z[M-k]))/2, Fo = -i (Z[k] - conj(Z[M-k]))/2 and
-// w_k = exp(-2*pi*i*k/L) passed in. `both` = false skips X[M-k] (k = 0: Nyquist).
-// Both outputs come out multiplied by the row's scale (folded into the 1/2).
+// w_k = exp(-2*pi*i*k/L). `both` = false skips X[M-k] (k = 0: Nyquist).
+// Both outputs come out multiplied by the row's scale, folded into the 1/2:
+// h = yrow.half = scale/2 is a power of two, and the caller passes hw = h*w_k.
+// With s = Z[k] + conj(Z[M-k]) and d = -i (Z[k] - conj(Z[M-k])), the outputs
+// are h*s + hw*d and conj(h*s - hw*d), an FMA per component. Scaling by a power
+// of two is exact, so these are the same numbers as scaling Fe and Fo first
+// (one multiply per component fewer).
 template <class Row>
-__device__ __forceinline__ void split_store(float2 zk, float2 zmk, float2 w, int k, int M,
+__device__ __forceinline__ void split_store(float2 zk, float2 zmk, float2 hw, int k, int M,
                                             bool both, const Row &yrow) {
-    const float2 zm = make_float2(zmk.x, -zmk.y);
     const float h = yrow.half;
-    const float2 fe = make_float2(h * (zk.x + zm.x), h * (zk.y + zm.y));
-    const float2 fo = make_float2(h * (zk.y - zm.y), -h * (zk.x - zm.x));
-    const float2 wf = cmul(w, fo);
-    yrow.put(k, cadd(fe, wf));
-    if (both) yrow.put(M - k, make_float2(fe.x - wf.x, wf.y - fe.y));
+    const float2 s = make_float2(zk.x + zmk.x, zk.y - zmk.y);
+    const float2 d = make_float2(zk.y + zmk.y, zmk.x - zk.x);
+    const float2 wf = cmul(hw, d);
+    yrow.put(k, fma2(make_float2(h, h), s, wf));
+    if (both) yrow.put(M - k, make_float2(fmaf(h, s.x, -wf.x), fmaf(-h, s.y, wf.y)));
+}
+
+// h*w for the power of two h = yrow.half (exact).
+__device__ __forceinline__ float2 scale_tw(float2 w, float h) {
+    return make_float2(w.x * h, w.y * h);
 }
 
 // Packets of 1024 samples (512 int8 pairs) kept for frame f of station s: all
