@@ -475,8 +475,8 @@ def main() -> None:
                 "alg_bytes_per_launch": dk["alg_bytes"], "frames_per_launch": PASS_FRAMES}
     if dom == "fengine":
         roofline["limiter"] = ("FP32 FFT arithmetic and shared-memory exchanges, not HBM: ncu on a "
-                               "256-frame launch saw the FP32 pipe 57 % busy, shared-memory "
-                               "wavefronts at 44 % and DRAM at 24 % of peak")
+                               "256-frame launch saw the FP32 pipe 56 % busy, shared-memory "
+                               "wavefronts at 46 % and DRAM at 25 % of peak")
 
     e2e = None
     if not args.no_e2e and rank == 0:
