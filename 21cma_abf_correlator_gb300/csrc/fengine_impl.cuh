@@ -332,8 +332,9 @@ struct FeCfg {
 
 // Two signed bytes (little-endian pair) -> two floats, exactly, without the
 // conversion unit: flipping the sign bit gives b + 128 in [0, 255]; placed in the
-// low byte of 0x4B000000 that is the float 2^23 + b + 128, and subtracting
-// 2^23 + 128 leaves b.
+// low byte of 0x4B000000 that is the float 2^23 + b + 128 (int8_pair_to_biased),
+// and subtracting B = 2^23 + 128 leaves b (int8_pair_to_float2). The first
+// passes keep the biased values and take B out in their first butterflies.
 constexpr float kInt8Bias = 8388736.0f;   // 2^23 + 128
 __device__ __forceinline__ float2 int8_pair_to_biased(uint16_t u) {
     const uint32_t x = static_cast<uint32_t>(u) ^ 0x8080u;
