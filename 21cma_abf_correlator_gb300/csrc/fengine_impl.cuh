@@ -42,12 +42,33 @@ namespace {
 template <int R>
 struct Dft;
 
+// The constant twiddles at odd multiples of pi/4 (m = 4, 12 in 32nds of a turn)
+// are sqrt(1/2) times a sum and a difference: a * exp(-2*pi*i*m/32) = r*u with
+// r = sqrt(1/2), u = (a.x + a.y, a.y - a.x) (m = 4) or (a.y - a.x, -(a.x + a.y))
+// (m = 12). A DFT stage passes u on ("pending"), and the next butterflies take
+// the factor r into their additions as FMAs (run_pend): two FP32 operations
+// fewer per such twiddle. `pend` has bit p set when v[p] holds such a u; it is
+// a compile-time constant once the enclosing loops are unrolled.
+constexpr float kSqrtHalf = 0.70710678118654752440f;
+__device__ __forceinline__ float2 w8_pending(float2 a, int m) {
+    return m == 4 ? make_float2(a.x + a.y, a.y - a.x) : make_float2(a.y - a.x, -a.x - a.y);
+}
+
 template <>
 struct Dft<2> {
     static __device__ __forceinline__ void run(float2 *v) {
         const float2 a = v[0], b = v[1];
         v[0] = cadd(a, b);
         v[1] = csub(a, b);
+    }
+    static __device__ __forceinline__ void run_pend(float2 *v, int pend) {
+        if (pend == 0b10) {
+            const float2 a = v[0], b = v[1];
+            v[0] = fma2(make_float2(kSqrtHalf, kSqrtHalf), b, a);
+            v[1] = fma2(make_float2(-kSqrtHalf, -kSqrtHalf), b, a);
+        } else {
+            run(v);
+        }
     }
 };
 
@@ -70,6 +91,25 @@ struct Dft<4> {
     static __device__ __forceinline__ void run_biased(float2 *v, float2 two_b) {
         finish(cadd(v[0], csub(v[2], two_b)), csub(v[0], v[2]), cadd(v[1], csub(v[3], two_b)),
                csub(v[1], v[3]), v);
+    }
+    // pend: 0, 0b0100 (v[2] pending) or 0b1010 (v[1] and v[3] pending).
+    static __device__ __forceinline__ void run_pend(float2 *v, int pend) {
+        const float2 rr = make_float2(kSqrtHalf, kSqrtHalf);
+        const float2 nrr = make_float2(-kSqrtHalf, -kSqrtHalf);
+        if (pend == 0b0100) {
+            finish(fma2(rr, v[2], v[0]), fma2(nrr, v[2], v[0]), cadd(v[1], v[3]), csub(v[1], v[3]),
+                   v);
+        } else if (pend == 0b1010) {
+            // s13 = r*p and d13 = r*q
+            const float2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+            const float2 p = cadd(v[1], v[3]), q = csub(v[1], v[3]);
+            v[0] = fma2(rr, p, s02);
+            v[2] = fma2(nrr, p, s02);
+            v[1] = make_float2(fmaf(kSqrtHalf, q.y, d02.x), fmaf(-kSqrtHalf, q.x, d02.y));
+            v[3] = make_float2(fmaf(-kSqrtHalf, q.y, d02.x), fmaf(kSqrtHalf, q.x, d02.y));
+        } else {
+            run(v);
+        }
     }
 };
 
@@ -192,33 +232,49 @@ struct Dft<15> {
 };
 
 // R = 4 x (R/4): n = (R/4)*n1 + n2, k = k1 + 4*k2. BIASED: the inputs still
-// carry the int8 unpacking's offset (Dft<4>::run_biased).
+// carry the int8 unpacking's offset (Dft<4>::run_biased). pend: inputs holding
+// a pending u (w8_pending); the twiddles between the two stages at odd
+// multiples of pi/4 are passed on pending to the second stage.
 template <int R>
 struct Dft {
     static_assert(R == 8 || R == 16 || R == 32, "radix");
     static constexpr int R2 = R / 4;
     template <bool BIASED = false>
-    static __device__ __forceinline__ void run(float2 *v, float2 two_b = float2{}) {
+    static __device__ __forceinline__ void run(float2 *v, float2 two_b = float2{}, int pend = 0) {
         float2 b[R2][4];
 #pragma unroll
         for (int n2 = 0; n2 < R2; ++n2) {
             float2 t[4] = {v[n2], v[R2 + n2], v[2 * R2 + n2], v[3 * R2 + n2]};
-            if constexpr (BIASED)
+            if constexpr (BIASED) {
                 Dft<4>::run_biased(t, two_b);
-            else
-                Dft<4>::run(t);
+            } else {
+                const int sub = ((pend >> n2) & 1) | (((pend >> (R2 + n2)) & 1) << 1) |
+                                (((pend >> (2 * R2 + n2)) & 1) << 2) |
+                                (((pend >> (3 * R2 + n2)) & 1) << 3);
+                Dft<4>::run_pend(t, sub);
+            }
 #pragma unroll
-            for (int k1 = 0; k1 < 4; ++k1) b[n2][k1] = mul_w32(t[k1], n2 * k1 * (32 / R));
+            for (int k1 = 0; k1 < 4; ++k1) {
+                const int m = (n2 * k1 * (32 / R)) & 31;
+                b[n2][k1] = (m & 7) == 4 ? w8_pending(t[k1], m) : mul_w32(t[k1], m);
+            }
         }
 #pragma unroll
         for (int k1 = 0; k1 < 4; ++k1) {
             float2 t[R2];
+            int sub = 0;
 #pragma unroll
-            for (int n2 = 0; n2 < R2; ++n2) t[n2] = b[n2][k1];
-            Dft<R2>::run(t);
+            for (int n2 = 0; n2 < R2; ++n2) {
+                t[n2] = b[n2][k1];
+                if (((n2 * k1 * (32 / R)) & 7) == 4) sub |= 1 << n2;
+            }
+            Dft<R2>::run_pend(t, sub);
 #pragma unroll
             for (int k2 = 0; k2 < R2; ++k2) v[k1 + 4 * k2] = t[k2];
         }
+    }
+    static __device__ __forceinline__ void run_pend(float2 *v, int pend) {
+        run<false>(v, float2{}, pend);
     }
 };
 
