@@ -42,16 +42,94 @@ namespace {
 template <int R>
 struct Dft;
 
-// The constant twiddles at odd multiples of pi/4 (m = 4, 12 in 32nds of a turn)
-// are sqrt(1/2) times a sum and a difference: a * exp(-2*pi*i*m/32) = r*u with
-// r = sqrt(1/2), u = (a.x + a.y, a.y - a.x) (m = 4) or (a.y - a.x, -(a.x + a.y))
-// (m = 12). A DFT stage passes u on ("pending"), and the next butterflies take
-// the factor r into their additions as FMAs (run_pend): two FP32 operations
-// fewer per such twiddle. `pend` has bit p set when v[p] holds such a u; it is
-// a compile-time constant once the enclosing loops are unrolled.
-constexpr float kSqrtHalf = 0.70710678118654752440f;
-__device__ __forceinline__ float2 w8_pending(float2 a, int m) {
-    return m == 4 ? make_float2(a.x + a.y, a.y - a.x) : make_float2(a.y - a.x, -a.x - a.y);
+// Scaled elements. Inside the radix-8/16/32 DFTs an element is kept as
+// (s.x * v.x, s.y * v.y), where the lanes' scales s are compile-time constants
+// once the loops are unrolled. A constant twiddle c - i*s in tangent form,
+// c*(x + t*y, y - t*x) with t = s/c (or the cotangent form when |s| > |c|),
+// costs two FMAs instead of a complex product's four and leaves its cosine (or
+// sine) in the scales; the butterflies that follow take the scales in as FMAs
+// in place of their additions, choosing the side whose scale is +-1, so the
+// DFT's outputs come out with unit scales. Two FP32 operations fewer per
+// constant twiddle; the rounding is that of the FMA forms.
+struct Sv {
+    float2 v, s;
+};
+
+// One lane of as*av + bs*bv in one operation: the new (v, s).
+__device__ __forceinline__ void sv_lane(float av, float as, float bv, float bs, float &v,
+                                        float &s) {
+    if (as == bs) {
+        v = av + bv;
+        s = as;
+    } else if (as == -bs) {
+        v = av - bv;
+        s = as;
+    } else if (fabsf(as) == 1.0f || fabsf(bs) != 1.0f) {
+        v = fmaf(bs / as, bv, av);
+        s = as;
+    } else {
+        v = fmaf(as / bs, av, bv);
+        s = bs;
+    }
+}
+// Whether sv_lane keeps a's scale (a is the addend).
+__host__ __device__ constexpr bool sv_keeps_a(float as, float bs) {
+    return as == bs || as == -bs || as == 1.0f || as == -1.0f || (bs != 1.0f && bs != -1.0f);
+}
+
+// a + b (minus: a - b); one packed instruction where both lanes keep a's scale.
+__device__ __forceinline__ Sv sv_comb(const Sv &a, const Sv &b, bool minus) {
+    const float bsx = minus ? -b.s.x : b.s.x, bsy = minus ? -b.s.y : b.s.y;
+    if (sv_keeps_a(a.s.x, bsx) && sv_keeps_a(a.s.y, bsy)) {
+        const float qx = bsx / a.s.x, qy = bsy / a.s.y;
+        float2 v;
+        if (qx == 1.0f && qy == 1.0f)
+            v = cadd(a.v, b.v);
+        else if (qx == -1.0f && qy == -1.0f)
+            v = csub(a.v, b.v);
+        else
+            v = fma2(make_float2(qx, qy), b.v, a.v);
+        return {v, a.s};
+    }
+    Sv r;
+    sv_lane(a.v.x, a.s.x, b.v.x, bsx, r.v.x, r.s.x);
+    sv_lane(a.v.y, a.s.y, b.v.y, bsy, r.v.y, r.s.y);
+    return r;
+}
+// a - i*b (minus: a + i*b), lane by lane (the swap keeps it out of the packed form).
+__device__ __forceinline__ Sv sv_comb_mi(const Sv &a, const Sv &b, bool minus) {
+    // -i*b = (b.y, -b.x)
+    const float bsx = minus ? -b.s.y : b.s.y, bsy = minus ? b.s.x : -b.s.x;
+    Sv r;
+    sv_lane(a.v.x, a.s.x, b.v.y, bsx, r.v.x, r.s.x);
+    sv_lane(a.v.y, a.s.y, b.v.x, bsy, r.v.y, r.s.y);
+    return r;
+}
+// a * exp(-2*pi*i*m/32), m a compile-time constant.
+__device__ __forceinline__ Sv sv_twiddle(const Sv &a, int m) {
+    m &= 31;
+    if (m == 0) return a;
+    if (m == 8) return {make_float2(a.v.y, a.v.x), make_float2(a.s.y, -a.s.x)};    // * -i
+    if (m == 16) return {a.v, make_float2(-a.s.x, -a.s.y)};
+    if (m == 24) return {make_float2(a.v.y, a.v.x), make_float2(-a.s.y, a.s.x)};   // * i
+    const float c = cos32(m), s = sin32(m);
+    if (fabsf(c) >= fabsf(s)) {
+        // re = c*sx*(vx + t*(sy/sx)*vy), im = c*sy*(vy - t*(sx/sy)*vx)
+        const float t = s / c;
+        return {make_float2(fmaf(t * a.s.y / a.s.x, a.v.y, a.v.x),
+                            fmaf(-t * a.s.x / a.s.y, a.v.x, a.v.y)),
+                make_float2(c * a.s.x, c * a.s.y)};
+    }
+    // re = s*sy*(vy + u*(sx/sy)*vx), im = -s*sx*(vx - u*(sy/sx)*vy), u = c/s
+    const float u = c / s;
+    return {make_float2(fmaf(u * a.s.x / a.s.y, a.v.x, a.v.y),
+                        fmaf(-u * a.s.y / a.s.x, a.v.y, a.v.x)),
+            make_float2(s * a.s.y, -s * a.s.x)};
+}
+// The plain value (the scales are 1 at a DFT's outputs; this folds away then).
+__device__ __forceinline__ float2 sv_value(const Sv &a) {
+    return make_float2(a.s.x == 1.0f ? a.v.x : a.s.x * a.v.x,
+                       a.s.y == 1.0f ? a.v.y : a.s.y * a.v.y);
 }
 
 template <>
@@ -61,14 +139,10 @@ struct Dft<2> {
         v[0] = cadd(a, b);
         v[1] = csub(a, b);
     }
-    static __device__ __forceinline__ void run_pend(float2 *v, int pend) {
-        if (pend == 0b10) {
-            const float2 a = v[0], b = v[1];
-            v[0] = fma2(make_float2(kSqrtHalf, kSqrtHalf), b, a);
-            v[1] = fma2(make_float2(-kSqrtHalf, -kSqrtHalf), b, a);
-        } else {
-            run(v);
-        }
+    static __device__ __forceinline__ void run_sv(Sv *v) {
+        const Sv a = v[0], b = v[1];
+        v[0] = sv_comb(a, b, false);
+        v[1] = sv_comb(a, b, true);
     }
 };
 
@@ -92,24 +166,13 @@ struct Dft<4> {
         finish(cadd(v[0], csub(v[2], two_b)), csub(v[0], v[2]), cadd(v[1], csub(v[3], two_b)),
                csub(v[1], v[3]), v);
     }
-    // pend: 0, 0b0100 (v[2] pending) or 0b1010 (v[1] and v[3] pending).
-    static __device__ __forceinline__ void run_pend(float2 *v, int pend) {
-        const float2 rr = make_float2(kSqrtHalf, kSqrtHalf);
-        const float2 nrr = make_float2(-kSqrtHalf, -kSqrtHalf);
-        if (pend == 0b0100) {
-            finish(fma2(rr, v[2], v[0]), fma2(nrr, v[2], v[0]), cadd(v[1], v[3]), csub(v[1], v[3]),
-                   v);
-        } else if (pend == 0b1010) {
-            // s13 = r*p and d13 = r*q
-            const float2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
-            const float2 p = cadd(v[1], v[3]), q = csub(v[1], v[3]);
-            v[0] = fma2(rr, p, s02);
-            v[2] = fma2(nrr, p, s02);
-            v[1] = make_float2(fmaf(kSqrtHalf, q.y, d02.x), fmaf(-kSqrtHalf, q.x, d02.y));
-            v[3] = make_float2(fmaf(-kSqrtHalf, q.y, d02.x), fmaf(kSqrtHalf, q.x, d02.y));
-        } else {
-            run(v);
-        }
+    static __device__ __forceinline__ void run_sv(Sv *v) {
+        const Sv s02 = sv_comb(v[0], v[2], false), d02 = sv_comb(v[0], v[2], true);
+        const Sv s13 = sv_comb(v[1], v[3], false), d13 = sv_comb(v[1], v[3], true);
+        v[0] = sv_comb(s02, s13, false);
+        v[2] = sv_comb(s02, s13, true);
+        v[1] = sv_comb_mi(d02, d13, false);   // d02 - i*d13
+        v[3] = sv_comb_mi(d02, d13, true);    // d02 + i*d13
     }
 };
 
@@ -231,50 +294,67 @@ struct Dft<15> {
     }
 };
 
-// R = 4 x (R/4): n = (R/4)*n1 + n2, k = k1 + 4*k2. BIASED: the inputs still
-// carry the int8 unpacking's offset (Dft<4>::run_biased). pend: inputs holding
-// a pending u (w8_pending); the twiddles between the two stages at odd
-// multiples of pi/4 are passed on pending to the second stage.
+// R = 4 x (R/4): n = (R/4)*n1 + n2, k = k1 + 4*k2, on scaled elements (Sv) with
+// the constant twiddles between the two stages in tangent form. BIASED: the
+// inputs still carry the int8 unpacking's offset (Dft<4>::run_biased).
 template <int R>
 struct Dft {
     static_assert(R == 8 || R == 16 || R == 32, "radix");
     static constexpr int R2 = R / 4;
     template <bool BIASED = false>
-    static __device__ __forceinline__ void run(float2 *v, float2 two_b = float2{}, int pend = 0) {
-        float2 b[R2][4];
+    static __device__ __forceinline__ void run(float2 *v, float2 two_b = float2{}) {
+        Sv e[R];
 #pragma unroll
         for (int n2 = 0; n2 < R2; ++n2) {
-            float2 t[4] = {v[n2], v[R2 + n2], v[2 * R2 + n2], v[3 * R2 + n2]};
+            Sv t[4];
             if constexpr (BIASED) {
-                Dft<4>::run_biased(t, two_b);
+                float2 f[4] = {v[n2], v[R2 + n2], v[2 * R2 + n2], v[3 * R2 + n2]};
+                Dft<4>::run_biased(f, two_b);
+#pragma unroll
+                for (int k1 = 0; k1 < 4; ++k1) t[k1] = {f[k1], make_float2(1.0f, 1.0f)};
             } else {
-                const int sub = ((pend >> n2) & 1) | (((pend >> (R2 + n2)) & 1) << 1) |
-                                (((pend >> (2 * R2 + n2)) & 1) << 2) |
-                                (((pend >> (3 * R2 + n2)) & 1) << 3);
-                Dft<4>::run_pend(t, sub);
+#pragma unroll
+                for (int n1 = 0; n1 < 4; ++n1) t[n1] = {v[n1 * R2 + n2], make_float2(1.0f, 1.0f)};
+                Dft<4>::run_sv(t);
             }
 #pragma unroll
-            for (int k1 = 0; k1 < 4; ++k1) {
-                const int m = (n2 * k1 * (32 / R)) & 31;
-                b[n2][k1] = (m & 7) == 4 ? w8_pending(t[k1], m) : mul_w32(t[k1], m);
-            }
+            for (int k1 = 0; k1 < 4; ++k1) e[n2 * 4 + k1] = sv_twiddle(t[k1], n2 * k1 * (32 / R));
+        }
+        second_stage(e, v);
+    }
+    // Inputs already scaled (the inner DFT of a larger one).
+    static __device__ __forceinline__ void run_sv(Sv *x) {
+        Sv e[R];
+#pragma unroll
+        for (int n2 = 0; n2 < R2; ++n2) {
+            Sv t[4] = {x[n2], x[R2 + n2], x[2 * R2 + n2], x[3 * R2 + n2]};
+            Dft<4>::run_sv(t);
+#pragma unroll
+            for (int k1 = 0; k1 < 4; ++k1) e[n2 * 4 + k1] = sv_twiddle(t[k1], n2 * k1 * (32 / R));
         }
 #pragma unroll
         for (int k1 = 0; k1 < 4; ++k1) {
-            float2 t[R2];
-            int sub = 0;
+            Sv t[R2];
 #pragma unroll
-            for (int n2 = 0; n2 < R2; ++n2) {
-                t[n2] = b[n2][k1];
-                if (((n2 * k1 * (32 / R)) & 7) == 4) sub |= 1 << n2;
-            }
-            Dft<R2>::run_pend(t, sub);
+            for (int n2 = 0; n2 < R2; ++n2) t[n2] = e[n2 * 4 + k1];
+            Dft<R2>::run_sv(t);
 #pragma unroll
-            for (int k2 = 0; k2 < R2; ++k2) v[k1 + 4 * k2] = t[k2];
+            for (int k2 = 0; k2 < R2; ++k2) x[k1 + 4 * k2] = t[k2];
         }
     }
-    static __device__ __forceinline__ void run_pend(float2 *v, int pend) {
-        run<false>(v, float2{}, pend);
+
+  private:
+    // e[n2*4 + k1] (twiddled first-stage outputs) -> v[k1 + 4*k2], unit scales.
+    static __device__ __forceinline__ void second_stage(Sv *e, float2 *v) {
+#pragma unroll
+        for (int k1 = 0; k1 < 4; ++k1) {
+            Sv t[R2];
+#pragma unroll
+            for (int n2 = 0; n2 < R2; ++n2) t[n2] = e[n2 * 4 + k1];
+            Dft<R2>::run_sv(t);
+#pragma unroll
+            for (int k2 = 0; k2 < R2; ++k2) v[k1 + 4 * k2] = sv_value(t[k2]);
+        }
     }
 };
 
