@@ -475,8 +475,8 @@ def main() -> None:
                 "alg_bytes_per_launch": dk["alg_bytes"], "frames_per_launch": PASS_FRAMES}
     if dom == "fengine":
         roofline["limiter"] = ("FP32 FFT arithmetic and shared-memory exchanges, not HBM: ncu on a "
-                               "256-frame launch saw the FP32 pipe 56 % busy, shared-memory "
-                               "wavefronts at 46 % and DRAM at 25 % of peak")
+                               "256-frame launch saw the FP32 pipe 52 % busy, shared-memory "
+                               "wavefronts at 47 % and DRAM at 25 % of peak")
 
     e2e = None
     if not args.no_e2e and rank == 0:
@@ -1000,8 +1000,8 @@ def run_e2e(pkg, w, x, mask, xmode, args, torch) -> dict:
         while c.lib.corr_rows_fetch_ready(c.ctx) == pkg.abi.CORR_ERR_BUSY:
             time.sleep(20e-6)
 
-    # wall clock on the host: the median of three rounds, so that one hiccup of
-    # the host's scheduler does not stand for the path
+    # wall clock on the host: the median of five rounds, so that a hiccup or two
+    # of the host's scheduler does not stand for the path
     k = max(2, args.steps // 2)
     medians = {}
     for blocking in (True, False):
@@ -1009,7 +1009,7 @@ def run_e2e(pkg, w, x, mask, xmode, args, torch) -> dict:
             integration(i, blocking)
         wait_fetches()
         rounds = []
-        for _ in range(3):
+        for _ in range(5):
             t0 = time.perf_counter()
             for i in range(k):
                 integration(i, blocking)
